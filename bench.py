@@ -1,0 +1,456 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 radix hot path.
+
+Headline workload: stable LSD radix sort of 100,000,000 uniform uint32 keys
+((uint32)std::mt19937_64(1234)(), the reference's recipe) on one GPU, 8-bit
+digits (4 passes).  One step = one sort of the whole array with the keys
+already resident in HBM; the input is restored from a pristine device copy
+before each step, outside the step's CUDA events.  The 400 MB input is
+larger than the 129 MB L2, so no L2 flush is needed between steps.
+
+Printed as one JSON line (rank 0):
+  value       keys/s over the device-resident sort (CUDA events per step)
+  e2e         keys/s through the reference-facing C ABI (pa_sort_u32) with
+              pinned HOST buffers: host->device copy, sort, device->host copy
+  roofline    the dominant kernel (one onesweep digit pass): algorithmic
+              bytes per launch (8 bytes/key: read + write each key once)
+              over its CUDA-event duration, against the measured HBM copy
+              bandwidth in MEASURED_PEAKS.json
+  cpu_baseline the reference's own SortRadixPar (compiled unchanged, TBB
+              stand-in thread pool) on this host's cores, same input
+  extras      presorted / constant sorts, 64-bit key+payload and float32
+              sorts, low-digit histogram, select k = n/2 and 64-bit sum at
+              100M, each with its own bytes-moved roofline fraction
+
+--impl reference times the reference's CPU SortRadixPar on the same
+workload (rank 0 only under torchrun; other ranks exit without work).
+With --gpus N > 1 every rank sorts its own replica (the path does not
+shard): value = all keys sorted / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "uint32 keys/s sorted at 100M vs HBM roofline; batched/served keys/s + p99 latency"
+UNIT = "keys/s"
+PROFILE_TRAFFIC = ROOT / "profiles" / "onesweep_pass_u32_100m_traffic.txt"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--n", type=int, default=100_000_000)
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--cpu-steps", type=int, default=5)
+    p.add_argument("--no-extras", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks: NVML read through ctypes (settings are only read, never changed)
+# ---------------------------------------------------------------------------
+REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+           0x80: "hw_power_brake_slowdown", 0x2: "applications_clocks_setting"}
+
+
+class ClockSampler:
+    def __init__(self, cuda_index: int, period_s: float = 0.005):
+        self.samples: list[tuple[int, int]] = []
+        self.max_mhz = None
+        self.period = period_s
+        self._stop = threading.Event()
+        self._thread = None
+        self.nvml = None
+        self.handle = None
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                raise OSError("nvmlInit failed")
+            h = ctypes.c_void_p()
+            bus = None
+            try:
+                import torch
+                pr = torch.cuda.get_device_properties(cuda_index)
+                bus = f"{pr.pci_domain_id:08x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0".encode()
+            except Exception:
+                bus = None
+            ok = bus is not None and nv.nvmlDeviceGetHandleByPciBusId_v2(bus, ctypes.byref(h)) == 0
+            if not ok and nv.nvmlDeviceGetHandleByIndex_v2(cuda_index, ctypes.byref(h)) != 0:
+                raise OSError("no NVML handle")
+            self.nvml, self.handle = nv, h
+            mx = ctypes.c_uint()
+            if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = mx.value
+        except OSError:
+            self.nvml = None
+
+    def _read(self):
+        mhz = ctypes.c_uint()
+        rs = ctypes.c_ulonglong()
+        self.nvml.nvmlDeviceGetClockInfo(self.handle, 1, ctypes.byref(mhz))
+        self.nvml.nvmlDeviceGetCurrentClocksEventReasons(self.handle, ctypes.byref(rs))
+        return mhz.value, rs.value
+
+    def _loop(self):
+        while not self._stop.is_set():
+            self.samples.append(self._read())
+            time.sleep(self.period)
+
+    def __enter__(self):
+        if self.nvml is not None:
+            self._thread = threading.Thread(target=self._loop, daemon=True)
+            self._thread.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._thread:
+            self._thread.join()
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["nvml unavailable"], "samples": 0}
+        mhz = [m for m, _ in self.samples]
+        seen = 0
+        for _, r in self.samples:
+            seen |= r
+        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(v for k, v in REASONS.items() if seen & k), "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+def measured_peak_gbs() -> tuple[float, str]:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def profiled_traffic_per_launch() -> float | None:
+    """dram read+write bytes per onesweep launch from the committed ncu summary."""
+    if not PROFILE_TRAFFIC.exists():
+        return None
+    for line in PROFILE_TRAFFIC.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_reference_sort(keys: np.ndarray, steps: int, warmup: int) -> dict:
+    """The reference's SortRadixPar(a, tmp, n) on this host; median of steps."""
+    import oracle
+    from oracle import build as obuild
+    obuild.build_ref()
+    ref = oracle.ref()
+    n = keys.size
+    a = np.empty_like(keys)
+    tmp = np.empty_like(keys)
+    if ref is not None:
+        kind, cores = "reference", ref.threads()
+        run = lambda: ref.sort_radix_par(a, tmp)  # noqa: E731
+        what = "SortRadixPar(a, tmp, n) compiled from the reference headers with a thread-pool TBB stand-in"
+    else:
+        port = oracle.port()
+        kind, cores = "port", 1
+        run = lambda: port.sort(a)  # noqa: E731
+        what = "oracle restatement (single thread)"
+    times = []
+    for i in range(warmup + steps):
+        np.copyto(a, keys)
+        tmp[:] = 0  # page in the scratch buffer as the reference benchmark does
+        t0 = time.perf_counter()
+        run()
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+    med = statistics.median(times)
+    return {"value": n / med, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"{what}; {n} uniform uint32 keys (mt19937_64 seed 1234); median of {steps} after {warmup} "
+                      f"warm-up; {med * 1e3:.1f} ms per sort",
+            "ms": [t * 1e3 for t in times]}
+
+
+def reference_arm(args) -> None:
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    from parallelalgorithms_gb300 import build as pabuild
+    pabuild.build()
+    from parallelalgorithms_gb300 import workloads
+    keys = workloads.uniform_u32(args.n)
+    cb = cpu_reference_sort(keys, args.steps, args.warmup)
+    med_s = args.n / cb["value"]
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": med_s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": f"LSD radix sort of {args.n} uniform uint32 keys, 8-bit digits",
+                       "keys": args.n, "key_type": "uint32", "distribution": "uniform mt19937_64(1234)",
+                       "l2": "inputs (400 MB) larger than L2"},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def gb300_arm(args) -> None:
+    import torch
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from parallelalgorithms_gb300 import build as pabuild
+    pabuild.build()
+    import parallelalgorithms_gb300 as pa
+    from parallelalgorithms_gb300 import _native, workloads
+
+    lib = pa.lib()
+    n = args.n
+    keys = workloads.uniform_u32(n)
+    src = torch.from_numpy(keys.view(np.int32)).cuda()
+    d_keys = torch.empty_like(src)
+    d_tmp = torch.empty_like(src)
+    stream = torch.cuda.current_stream()
+    opts = _native.opts(stream.cuda_stream, async_device=True)
+    P = ctypes.c_void_p
+
+    def sort_once():
+        rc = lib.pa_sort_u32(P(d_keys.data_ptr()), P(d_tmp.data_ptr()), n, opts)
+        if rc:
+            raise RuntimeError(f"pa_sort_u32 failed: {lib.pa_last_error_message().decode()}")
+
+    for _ in range(args.warmup):
+        d_keys.copy_(src)
+        sort_once()
+    _native.call("pa_stream_check", P(stream.cuda_stream))
+    flipped = d_keys ^ torch.tensor(-2147483648, dtype=torch.int32, device=d_keys.device)
+    if not bool(torch.all(flipped[1:] >= flipped[:-1])):
+        raise RuntimeError("warm-up sort result is not sorted")
+    del flipped
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    with sampler:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            d_keys.copy_(src)
+            starts[i].record(stream)
+            sort_once()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    _native.call("pa_stream_check", P(stream.cuda_stream))
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = statistics.mean(step_ms)
+    ms_max = ms
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = n * world / (ms_max / 1e3)
+
+    # per-kernel device times (same stream, CUDA events between launches)
+    phases = np.zeros(16, np.float32)
+    reps = 10
+    acc = np.zeros(16, np.float64)
+    for _ in range(reps):
+        d_keys.copy_(src)
+        _native.call("pa_sort_timed", 0, P(d_keys.data_ptr()), P(d_tmp.data_ptr()), None, None, n,
+                     P(phases.ctypes.data), 16, _native.opts(stream.cuda_stream))
+        acc += phases
+    acc /= reps
+    hist_ms, scan_ms = float(acc[0]), float(acc[1])
+    pass_ms = [float(x) for x in acc[2:6]]
+    copy_ms = float(acc[6])
+    peak, peak_kind = measured_peak_gbs()
+    pass_avg = statistics.mean(pass_ms)
+    achieved = 8.0 * n / (pass_avg / 1e3) / 1e9
+    traffic = profiled_traffic_per_launch()
+    roofline = {"bound": "hbm", "kernel": "onesweep digit pass (uint32 keys, 8-bit digit)", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
+                else "fallback 6800 GB/s",
+                "bytes_per_launch": 8 * n, "launch_ms": pass_avg}
+    sort_bytes = 36.0 * n
+    whole = {"bytes_per_key": 36, "achieved_gbs": sort_bytes / (ms / 1e3) / 1e9,
+             "frac": sort_bytes / (ms / 1e3) / 1e9 / peak,
+             "phase_ms": {"histogram": hist_ms, "scan": scan_ms, "passes": pass_ms, "final_copy": copy_ms}}
+
+    # end to end through the C ABI with pinned host buffers
+    h_src = workloads.uniform_u32(n, pinned=True)
+    h_buf = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    h_keys = h_buf.numpy().view(np.uint32)
+    e2e_times = []
+    for i in range(args.e2e_steps + 1):
+        np.copyto(h_keys, h_src)
+        t0 = time.perf_counter()
+        _native.call("pa_sort_u32", P(h_keys.ctypes.data), None, n, None)
+        dt = time.perf_counter() - t0
+        if i > 0:
+            e2e_times.append(dt)
+    if not np.all(h_keys[1:] >= h_keys[:-1]):
+        raise RuntimeError("end-to-end sort result is not sorted")
+    e2e_med = statistics.median(e2e_times)
+    e2e = {"value": n / e2e_med, "unit": UNIT, "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n,
+           "ms_per_step": e2e_med * 1e3, "api": "pa_sort_u32 (C ABI) on pinned host buffers, synchronous"}
+
+    extras = {} if args.no_extras else run_extras(pa, lib, _native, workloads, n, stream, peak)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_reference_sort(keys, args.cpu_steps, 1)
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    launches_per_step = 1 + 1 + 4 + 1  # histogram, scan, 4 digit passes, final copy
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": f"LSD radix sort of {n} uniform uint32 keys (mt19937_64 seed 1234), "
+                                   "8-bit digits, 4 passes, device-resident",
+                       "keys_per_gpu": n, "key_type": "uint32", "digit_bits": 8,
+                       "l2": "inputs (400 MB) larger than L2; no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "step_timing": "CUDA events around each sort; input restored from a pristine device copy "
+                                      "before each step, outside the events",
+                       "wall_ms_per_step_incl_restore": wall * 1e3 / args.steps},
+            "roofline": roofline, "sort_roofline": whole, "e2e": e2e, "cpu_baseline": cpu,
+            "gpu_launches": launches_per_step * args.steps, "clocks": sampler.summary(), "extras": extras,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def _time_device(fn, reps: int, stream, restore=None) -> float:
+    import torch
+    ts = []
+    for _ in range(reps):
+        if restore:
+            restore()
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        fn()
+        e.record(stream)
+        torch.cuda.synchronize()
+        ts.append(s.elapsed_time(e))
+    return statistics.median(ts)
+
+
+def run_extras(pa, lib, _native, workloads, n, stream, peak) -> dict:
+    """Other 100M workloads of the same path, device-resident, median of 5."""
+    import torch
+    P = ctypes.c_void_p
+    o = _native.opts(stream.cuda_stream, async_device=True)
+    out = {}
+
+    def dev(a):
+        return torch.from_numpy(a.view({4: np.int32, 8: np.int64}[a.dtype.itemsize])).cuda()
+
+    def sort_case(name, keys, vals=None, fn="pa_sort_u32", bytes_per_key=36):
+        src = dev(keys)
+        k = torch.empty_like(src)
+        tk = torch.empty_like(src)
+        v = tv = vsrc = None
+        if vals is not None:
+            vsrc = dev(vals)
+            v = torch.empty_like(vsrc)
+            tv = torch.empty_like(vsrc)
+
+        def restore():
+            k.copy_(src)
+            if vals is not None:
+                v.copy_(vsrc)
+
+        if vals is None:
+            f = lambda: _native.call(fn, P(k.data_ptr()), P(tk.data_ptr()), n, o)  # noqa: E731
+        else:
+            f = lambda: _native.call(fn, P(k.data_ptr()), P(v.data_ptr()), P(tk.data_ptr()),  # noqa: E731
+                                     P(tv.data_ptr()), n, o)
+        restore()
+        f()
+        ms = _time_device(f, 5, stream, restore)
+        _native.call("pa_stream_check", P(stream.cuda_stream))
+        gbs = bytes_per_key * n / (ms / 1e3) / 1e9
+        out[name] = {"ms": ms, "keys_per_s": n / (ms / 1e3), "bytes_per_key": bytes_per_key,
+                     "achieved_gbs": gbs, "frac": gbs / peak}
+        del src, k, tk, v, tv, vsrc
+        torch.cuda.empty_cache()
+
+    sort_case("sort_u32_presorted", workloads.presorted_u32(n))
+    sort_case("sort_u32_constant42", workloads.constant_u32(n, 42))
+    sort_case("sort_kv_u64_uniform_u32payload", workloads.uniform_u64(n), np.arange(n, dtype=np.uint32),
+              "pa_sort_kv_u64", 200)
+    sort_case("sort_kv_u64_zipf_u32payload", workloads.zipf_u64(n), np.arange(n, dtype=np.uint32),
+              "pa_sort_kv_u64", 200)
+    sort_case("sort_f32_normal_specials", workloads.normal_specials_f32(n).view(np.uint32), None, "pa_sort_f32", 36)
+
+    for dname, keys in (("uniform", workloads.uniform_u32(n)), ("presorted", workloads.presorted_u32(n)),
+                        ("constant42", workloads.constant_u32(n, 42))):
+        d = dev(keys)
+        hist = torch.zeros(256, dtype=torch.int64, device="cuda")
+        res = torch.zeros(1, dtype=torch.int64, device="cuda")
+        ms = _time_device(lambda: _native.call("pa_hist_one_byte_u32", P(d.data_ptr()), n, 0, P(hist.data_ptr()),
+                                               o), 5, stream)
+        out[f"histogram_low_digit_{dname}"] = {"ms": ms, "achieved_gbs": 4 * n / (ms / 1e3) / 1e9,
+                                               "frac": 4 * n / (ms / 1e3) / 1e9 / peak}
+        ms = _time_device(lambda: _native.call("pa_select_u32", P(d.data_ptr()), n, n // 2, P(res.data_ptr()), o),
+                          5, stream)
+        out[f"select_k_half_{dname}"] = {"ms": ms, "achieved_gbs_one_read": 4 * n / (ms / 1e3) / 1e9,
+                                         "frac_one_read": 4 * n / (ms / 1e3) / 1e9 / peak}
+        ms = _time_device(lambda: _native.call("pa_sum_u32", P(d.data_ptr()), n, P(res.data_ptr()), o), 5, stream)
+        out[f"sum_u64_{dname}"] = {"ms": ms, "achieved_gbs": 4 * n / (ms / 1e3) / 1e9,
+                                   "frac": 4 * n / (ms / 1e3) / 1e9 / peak}
+        _native.call("pa_stream_check", P(stream.cuda_stream))
+        del d
+    return out
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gb300_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,167 @@
+/*
+ * pa_gpu.h - C ABI of the GB300 radix hot path (sort, digit histograms,
+ * radix select, 64-bit sum) that replaces the CPU implementation in the
+ * reference library ParallelAlgorithms.
+ *
+ * Every entry point:
+ *   - is callable from C, C++ (see include/ParallelAlgorithms/ for inline
+ *     wrappers with the reference's own C++ signatures), or any FFI;
+ *   - takes plain pointers and sizes.  Each buffer may be HOST memory
+ *     (pageable or pinned; the call copies it to the GPU and back) or DEVICE
+ *     memory of the current CUDA device (used in place).  The kind is found
+ *     with cudaPointerGetAttributes;
+ *   - returns a pa_status code and never throws or aborts;
+ *   - is synchronous (returns after the results are in place) unless
+ *     opts->async_device is set and every buffer is device memory.
+ * There is no CPU fallback: with no usable GPU every call returns
+ * PA_ERR_NO_DEVICE.
+ *
+ * Citations name the reference entry point each function replaces
+ * (file:line within the reference project).
+ */
+#ifndef PA_GPU_H
+#define PA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pa_status {
+  PA_OK = 0,
+  PA_ERR_ARG = 1,       /* invalid argument (null buffer, k out of range, bad shift, ...) */
+  PA_ERR_OOM = 2,       /* device or pinned memory could not be allocated */
+  PA_ERR_CUDA = 3,      /* a CUDA runtime call failed; see pa_last_error_message() */
+  PA_ERR_TIMEOUT = 4,   /* a bounded device-side wait gave up; results are undefined */
+  PA_ERR_NO_DEVICE = 5  /* no CUDA device is usable */
+} pa_status;
+
+typedef struct pa_opts {
+  void* stream;      /* cudaStream_t to run on; NULL means the legacy default stream */
+  int async_device;  /* 1: if every buffer is device memory, return once the work is
+                        enqueued; bounded-wait failures are then reported by
+                        pa_stream_check(stream) */
+  int digit_bits;    /* radix digit width for sorts: 0 or 8 (the reference's
+                        PowerOfTwoRadix = 256) */
+  int reserved[4];   /* must be zero */
+} pa_opts;
+
+/* Human-readable name of a status code. */
+const char* pa_status_string(int status);
+/* Detail of the most recent failure on the calling thread ("" if none). */
+const char* pa_last_error_message(void);
+/* 1 if a CUDA device is usable from this process, else 0. */
+int pa_device_available(void);
+/* Synchronises `stream` and reports (then clears) any bounded-wait failure
+ * raised by earlier async_device calls on it. */
+int pa_stream_check(void* stream);
+/* Releases the cached device and pinned workspaces of every stream. */
+int pa_release_workspaces(void);
+
+/* ---- LSD radix sort ------------------------------------------------------
+ * Stable ascending sort of keys[0, n) in place.  tmp is caller scratch of n
+ * keys whose contents are clobbered; tmp == NULL lets the library use its
+ * own scratch.  The digit histograms of every pass are computed in one read
+ * of the keys before the digit passes.
+ *
+ * pa_sort_u32 replaces ParallelAlgorithms::SortRadixPar(unsigned* a,
+ *   unsigned* tmp_work_buff, size_t a_size, size_t parallelThreshold)
+ *   (RadixSortLsdParallel.h:367) and, with tmp == NULL,
+ *   SortRadixPar(unsigned* a, size_t a_size, size_t parallelThreshold)
+ *   (RadixSortLsdParallel.h:340), and SortRadixInnerPar<256,8>
+ *   (RadixSortLsdParallel.h:215).
+ * pa_sort_u64 / pa_sort_f32 / pa_sort_kv_* have no reference counterpart
+ *   (the reference sorts only unsigned 32-bit keys, RadixSortLsdParallel.h:216);
+ *   they are additive overloads.  Float keys sort by IEEE total order
+ *   (-0.0 before +0.0); payloads move with their keys, and equal keys keep
+ *   their input order.
+ */
+int pa_sort_u32(uint32_t* keys, uint32_t* tmp, size_t n, const pa_opts* opts);
+int pa_sort_u64(uint64_t* keys, uint64_t* tmp, size_t n, const pa_opts* opts);
+int pa_sort_f32(float* keys, float* tmp, size_t n, const pa_opts* opts);
+int pa_sort_kv_u32(uint32_t* keys, uint32_t* vals, uint32_t* tmp_keys, uint32_t* tmp_vals, size_t n,
+                   const pa_opts* opts);
+int pa_sort_kv_u64(uint64_t* keys, uint32_t* vals, uint64_t* tmp_keys, uint32_t* tmp_vals, size_t n,
+                   const pa_opts* opts);
+int pa_sort_kv_f32(float* keys, uint32_t* vals, float* tmp_keys, uint32_t* tmp_vals, size_t n,
+                   const pa_opts* opts);
+
+/* Sorts a[0, n) and leaves the sorted keys in BOTH a and b, which is the end
+ * state of RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase(a, b, a_size)
+ * (RadixSortLsdParallel.h:86-106) and of the intended (the reference's body
+ * is commented out, :503) RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase_DeRandomize
+ * (RadixSortLsdParallel.h:491). */
+int pa_sort_two_phase_u32(uint32_t* a, uint32_t* b, size_t n, const pa_opts* opts);
+
+/* Profiling form of the sorts above (key_kind: PA_KEY_U32 / PA_KEY_U64 /
+ * PA_KEY_F32; vals / tmp_vals may be NULL): same result, always synchronous,
+ * and phase_ms[i] receives the device time in milliseconds of each kernel,
+ * from CUDA events recorded between the launches: [0] the one-read digit
+ * histogram, [1] the bin-offset scan, [2 + p] digit pass p (one per key
+ * byte), [2 + passes] the final copy.  phase_cap bounds the entries written.
+ * GPU form of the per-phase timers the reference keeps commented out in its
+ * sort (RadixSortLsdParallel.h:255-258, 287, 307-308). */
+enum { PA_KEY_U32 = 0, PA_KEY_U64 = 1, PA_KEY_F32 = 2 };
+int pa_sort_timed(int key_kind, void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t n,
+                  float* phase_ms, int phase_cap, const pa_opts* opts);
+
+/* ---- digit histograms ----------------------------------------------------
+ * pa_hist_byte_components_u32: out[d * 256 + b] = number of keys in a[0, n)
+ *   whose byte d (d = 0..3, least significant first) equals b, from one read.
+ *   Replaces HistogramByteComponentsParallel<256,8>(a, l, r)
+ *   (HistogramParallel.h:249) with a = inArray + l, n = r - l + 1.
+ * pa_hist_one_byte_u32: out[b] = number of keys with ((key >> shift) & 255) == b;
+ *   shift must be < 32.  Replaces HistogramOneByteComponentParallel<256,8>(a,
+ *   l, r, shiftRight) (HistogramParallel.h:535).
+ * pa_hist_u8: out[b] = number of bytes equal to b.  Replaces
+ *   HistogramOneByteComponentParallel<256>(unsigned char a[], l, r)
+ *   (HistogramParallel.h:17) and its _2/_3/_4 variants (:58,:117,:184).
+ * pa_hist_quanta_u32: out[q * 256 + b] for q in [0, quanta): number of i in
+ *   [l, r] (r inclusive) with i / work_quanta == q and byte which_byte of a[i]
+ *   equal to b.  a is the array base (index 0).  Replaces
+ *   HistogramByteComponentsQCPar<256,8> (HistogramParallel.h:444).
+ * pa_start_of_bins_u32: out[q * 256 + b] = the output index of quantum q's
+ *   first key of bin b for byte `digit` over a[0, n).  Replaces
+ *   ComputeStartOfBinsPar<256,8> (RadixSortLsdParallel.h:108).
+ * out may be host or device memory; it is overwritten.
+ */
+int pa_hist_byte_components_u32(const uint32_t* a, size_t n, uint64_t* out, const pa_opts* opts);
+int pa_hist_one_byte_u32(const uint32_t* a, size_t n, unsigned shift, uint64_t* out, const pa_opts* opts);
+int pa_hist_u8(const uint8_t* a, size_t n, uint64_t* out, const pa_opts* opts);
+int pa_hist_quanta_u32(const uint32_t* a, size_t l, size_t r, size_t work_quanta, size_t quanta,
+                       unsigned which_byte, uint64_t* out, const pa_opts* opts);
+int pa_start_of_bins_u32(const uint32_t* a, size_t n, size_t work_quanta, size_t quanta, unsigned digit,
+                         uint64_t* out, const pa_opts* opts);
+
+/* ---- radix select ---------------------------------------------------------
+ * pa_select_u32 / pa_select_u64: *out = the k-th smallest (0-based) key of
+ *   a[0, n); a is not modified.  Requires k < n.
+ * pa_select_radix_u32: the reference's contract, SelectRadix(a, start,
+ *   length, k) (RadixSelect.h:139; SelectRadix(a, length, k) is start = 0,
+ *   RadixSelect.h:157): the (k - start)-th smallest of a[start, start + length)
+ *   with k an absolute index in that range, returned in *out AND stored to
+ *   a[k].  The reference also rearranges the rest of the range; here the rest
+ *   of `a` is left as it was.
+ */
+int pa_select_u32(const uint32_t* a, size_t n, size_t k, uint32_t* out, const pa_opts* opts);
+int pa_select_u64(const uint64_t* a, size_t n, size_t k, uint64_t* out, const pa_opts* opts);
+int pa_select_radix_u32(uint32_t* a, size_t start, size_t length, size_t k, uint32_t* out, const pa_opts* opts);
+
+/* ---- sum ------------------------------------------------------------------
+ * *out = sum of a[0, n) modulo 2^64 (exact; 32-bit inputs cannot wrap below
+ * 2^32 elements).  Replaces SumParallelNonRecursive(unsigned[], l, r)
+ * (SumParallel.h:261), SumParallelNonRecursive(unsigned long long[], l, r)
+ * (:285), SumParallel(unsigned long long[], l, r) (:162) and, reinterpreted as
+ * signed, SumParallel<unsigned>(...) -> long long (:207), with a = in_array + l
+ * and n = r - l.  An empty range sums to 0.  out may be host or device memory.
+ */
+int pa_sum_u32(const uint32_t* a, size_t n, uint64_t* out, const pa_opts* opts);
+int pa_sum_u64(const uint64_t* a, size_t n, uint64_t* out, const pa_opts* opts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PA_GPU_H */

@@ -1,0 +1,3 @@
+// Project-written stand-in: everything lives in tbb.h.
+#pragma once
+#include "tbb.h"

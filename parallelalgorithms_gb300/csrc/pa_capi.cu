@@ -1,0 +1,618 @@
+// The C ABI declared in include/pa_gpu.h.
+//
+// Responsibilities: argument checks, host/device classification of every
+// buffer, the per-stream device workspace (grow-only, reused across calls),
+// host<->device copies for host buffers, launching the kernel sequence of
+// each operation, and turning CUDA errors and device-side bounded-wait
+// failures into pa_status codes.  Calls are serialised by one mutex; work on
+// different streams uses different workspaces.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+
+#include "pa_gpu.h"
+#include "pa_common.cuh"
+#include "pa_kernels.cuh"
+
+namespace pa {
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int status, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return status;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    return set_error(PA_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+  }
+  return set_error(PA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define PA_CUDA(call)                                      \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);    \
+  } while (0)
+
+constexpr int kMaxEvents = 16;
+
+struct Workspace {
+  char* dev = nullptr;
+  size_t dev_cap = 0;
+  uint32_t* err = nullptr;       // device error word, zero between calls
+  uint32_t* err_host = nullptr;  // pinned mirror for reading it back
+  cudaEvent_t ev[kMaxEvents] = {};  // phase timing (created on first use)
+};
+
+std::mutex g_mu;
+std::map<std::pair<int, cudaStream_t>, Workspace> g_ws;
+
+// Lays out sub-buffers in one allocation, 256-byte aligned.  Run once with
+// base == nullptr to measure, then with the real base.
+struct Carve {
+  char* base;
+  size_t off = 0;
+  template <class T>
+  T* take(size_t count) {
+    off = (off + 255) & ~(size_t)255;
+    T* p = reinterpret_cast<T*>(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+
+int device_ready() {
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return set_error(PA_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+  }
+  return PA_OK;
+}
+
+int get_workspace(cudaStream_t stream, Workspace** out) {
+  int dev = 0;
+  PA_CUDA(cudaGetDevice(&dev));
+  Workspace& ws = g_ws[{dev, stream}];
+  if (!ws.err) {
+    PA_CUDA(cudaMalloc(&ws.err, 256));
+    PA_CUDA(cudaMemset(ws.err, 0, 256));
+    PA_CUDA(cudaMallocHost(&ws.err_host, sizeof(uint32_t)));
+  }
+  *out = &ws;
+  return PA_OK;
+}
+
+int ensure_dev(Workspace* ws, cudaStream_t stream, size_t bytes) {
+  if (bytes <= ws->dev_cap) return PA_OK;
+  PA_CUDA(cudaStreamSynchronize(stream));
+  if (ws->dev) PA_CUDA(cudaFree(ws->dev));
+  ws->dev = nullptr;
+  ws->dev_cap = 0;
+  const size_t cap = bytes + bytes / 8 + (1u << 20);
+  cudaError_t e = cudaMalloc(&ws->dev, cap);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(PA_ERR_OOM, "device workspace of %zu bytes: %s", cap, cudaGetErrorString(e));
+  }
+  ws->dev_cap = cap;
+  return PA_OK;
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return at.device == dev;
+  }
+  return false;
+}
+
+cudaStream_t stream_of(const pa_opts* o) { return o ? static_cast<cudaStream_t>(o->stream) : (cudaStream_t)0; }
+
+int check_opts(const pa_opts* o) {
+  if (!o) return PA_OK;
+  if (o->digit_bits != 0 && o->digit_bits != 8)
+    return set_error(PA_ERR_ARG, "digit_bits must be 0 or 8 (got %d)", o->digit_bits);
+  for (int r : o->reserved)
+    if (r != 0) return set_error(PA_ERR_ARG, "pa_opts.reserved must be zero");
+  return PA_OK;
+}
+
+// Synchronises and reports a device-side bounded-wait failure, if any.
+int finish(Workspace* ws, cudaStream_t stream, bool async_ok) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  if (async_ok) return PA_OK;
+  PA_CUDA(cudaMemcpyAsync(ws->err_host, ws->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+  PA_CUDA(cudaStreamSynchronize(stream));
+  const uint32_t err = *ws->err_host;
+  if (err) {
+    PA_CUDA(cudaMemsetAsync(ws->err, 0, sizeof(uint32_t), stream));
+    PA_CUDA(cudaStreamSynchronize(stream));
+    return set_error(PA_ERR_TIMEOUT, "device-side bounded wait gave up (code 0x%x); results are undefined", err);
+  }
+  return PA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Sort
+// ---------------------------------------------------------------------------
+// phase_ms (optional, phase_cap entries): device time of each kernel of the
+// sort from CUDA events recorded between launches on the call's stream:
+// [0] digit histogram, [1] scan, [2 + p] digit pass p, [2 + passes] final
+// copy.  Timing forces a synchronous call.
+int sort_impl(void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t n, int kb, bool is_float,
+              const pa_opts* opts, float* phase_ms = nullptr, int phase_cap = 0) {
+  if (int rc = check_opts(opts)) return rc;
+  if (n == 0) return PA_OK;
+  if (!keys) return set_error(PA_ERR_ARG, "keys is NULL");
+  if (tmp_vals && !vals) return set_error(PA_ERR_ARG, "tmp_vals given without vals");
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t stream = stream_of(opts);
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+
+  const bool has_vals = vals != nullptr;
+  const bool keys_dev = is_device_ptr(keys);
+  const bool tmp_dev = is_device_ptr(tmp);
+  const bool vals_dev = has_vals && is_device_ptr(vals);
+  const bool tvals_dev = has_vals && is_device_ptr(tmp_vals);
+  const int passes = kb;  // 8-bit digits: one pass per key byte
+  const size_t tile = onesweep_tile_keys(kb, has_vals);
+  const size_t tiles = ceil_div(n, tile);
+  const size_t sb = onesweep_status_bytes(n);
+
+  struct Layout {
+    void *d_keys, *d_tmp;
+    uint32_t *d_vals, *d_tvals;
+    unsigned long long* counts;
+    uint32_t* tile_ctr;
+    char* status;
+    unsigned long long* bin_start;
+    SortCtrl* ctrl;
+    size_t zero_off, zero_bytes;
+  } L{};
+  auto layout = [&](Carve& c) {
+    L.d_keys = keys_dev ? keys : c.take<char>(n * kb);
+    L.d_tmp = tmp_dev ? tmp : c.take<char>(n * kb);
+    if (has_vals) {
+      L.d_vals = vals_dev ? vals : c.take<uint32_t>(n);
+      L.d_tvals = tvals_dev ? tmp_vals : c.take<uint32_t>(n);
+    }
+    L.counts = c.take<unsigned long long>((size_t)passes * 256);
+    L.zero_off = (size_t)(reinterpret_cast<char*>(L.counts) - c.base);
+    L.tile_ctr = c.take<uint32_t>(passes);
+    L.status = c.take<char>((size_t)passes * tiles * 256 * sb);
+    L.zero_bytes = c.off - L.zero_off;
+    L.bin_start = c.take<unsigned long long>((size_t)passes * 256);
+    L.ctrl = c.take<SortCtrl>(1);
+  };
+  Carve measure{nullptr};
+  layout(measure);
+  if (int rc = ensure_dev(ws, stream, measure.off)) return rc;
+  Carve real{ws->dev};
+  layout(real);
+
+  const size_t key_bytes_total = n * (size_t)kb;
+  if (!keys_dev) PA_CUDA(cudaMemcpyAsync(L.d_keys, keys, key_bytes_total, cudaMemcpyHostToDevice, stream));
+  if (has_vals && !vals_dev)
+    PA_CUDA(cudaMemcpyAsync(L.d_vals, vals, n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+  PA_CUDA(cudaMemsetAsync(ws->dev + L.zero_off, 0, L.zero_bytes, stream));
+  const bool timed = phase_ms && phase_cap > 0;
+  int nev = 0;
+  auto mark = [&]() -> cudaError_t {
+    if (!timed || nev >= kMaxEvents) return cudaSuccess;
+    if (!ws->ev[nev]) {
+      cudaError_t e = cudaEventCreate(&ws->ev[nev]);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaEventRecord(ws->ev[nev++], stream);
+  };
+  PA_CUDA(mark());
+  PA_CUDA(launch_digit_counts(L.d_keys, n, kb, passes, 8, 0, 8, is_float, L.counts, stream));
+  PA_CUDA(mark());
+  PA_CUDA(launch_scan_digits(L.counts, passes, 8, n, is_float, true, L.bin_start, L.ctrl, stream));
+  PA_CUDA(mark());
+  for (int p = 0; p < passes; ++p) {
+    OnesweepArgs a{};
+    a.keys_a = L.d_keys;
+    a.keys_b = L.d_tmp;
+    a.vals_a = L.d_vals;
+    a.vals_b = L.d_tvals;
+    a.n = n;
+    a.shift = 8u * (uint32_t)p;
+    a.pass = p;
+    a.is_float = is_float ? 1 : 0;
+    a.bin_start = L.bin_start + (size_t)p * 256;
+    a.status = L.status + (size_t)p * tiles * 256 * sb;
+    a.tile_counter = L.tile_ctr + p;
+    a.ctrl = L.ctrl;
+    a.err = ws->err;
+    PA_CUDA(launch_onesweep_pass(a, kb, has_vals, stream));
+    PA_CUDA(mark());
+  }
+  PA_CUDA(launch_final_copy(L.d_keys, L.d_tmp, L.d_vals, L.d_tvals, n, kb, L.ctrl, stream));
+  PA_CUDA(mark());
+  if (!keys_dev) PA_CUDA(cudaMemcpyAsync(keys, L.d_keys, key_bytes_total, cudaMemcpyDeviceToHost, stream));
+  if (has_vals && !vals_dev)
+    PA_CUDA(cudaMemcpyAsync(vals, L.d_vals, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+  const bool all_dev = keys_dev && (!has_vals || vals_dev);
+  int rc = finish(ws, stream, !timed && opts && opts->async_device && all_dev);
+  if (rc == PA_OK && timed) {
+    for (int i = 0; i + 1 < nev && i < phase_cap; ++i) {
+      float ms = 0.f;
+      PA_CUDA(cudaEventElapsedTime(&ms, ws->ev[i], ws->ev[i + 1]));
+      phase_ms[i] = ms;
+    }
+  }
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Histograms
+// ---------------------------------------------------------------------------
+// One histogram call: `rows` x 256 counts of the digits selected by
+// (key_bytes, num_digits, shift0, step) over a[0, n) into out.
+int hist_impl(const void* a, size_t n, int kb, int num_digits, uint32_t shift0, uint32_t step, uint64_t* out,
+              const pa_opts* opts) {
+  if (int rc = check_opts(opts)) return rc;
+  if (!out) return set_error(PA_ERR_ARG, "out is NULL");
+  if (n && !a) return set_error(PA_ERR_ARG, "input is NULL");
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t stream = stream_of(opts);
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+  const bool in_dev = is_device_ptr(a);
+  const bool out_dev = is_device_ptr(out);
+  const size_t out_words = (size_t)num_digits * 256;
+  const void* d_in = nullptr;
+  unsigned long long* d_out = nullptr;
+  auto layout = [&](Carve& c) {
+    d_in = in_dev ? a : c.take<char>(n * kb);
+    d_out = out_dev ? reinterpret_cast<unsigned long long*>(out) : c.take<unsigned long long>(out_words);
+  };
+  Carve m{nullptr};
+  layout(m);
+  if (int rc = ensure_dev(ws, stream, m.off)) return rc;
+  Carve r{ws->dev};
+  layout(r);
+  if (!in_dev && n) PA_CUDA(cudaMemcpyAsync(const_cast<void*>(d_in), a, n * kb, cudaMemcpyHostToDevice, stream));
+  PA_CUDA(cudaMemsetAsync(d_out, 0, out_words * sizeof(uint64_t), stream));
+  PA_CUDA(launch_digit_counts(d_in, n, kb, num_digits, 8, shift0, step, false, d_out, stream));
+  if (!out_dev) PA_CUDA(cudaMemcpyAsync(out, d_out, out_words * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+  return finish(ws, stream, opts && opts->async_device && in_dev && out_dev);
+}
+
+// ---------------------------------------------------------------------------
+// Select
+// ---------------------------------------------------------------------------
+int select_impl(const void* a, size_t n, size_t k, int kb, void* out, const pa_opts* opts) {
+  if (int rc = check_opts(opts)) return rc;
+  if (!a || !out) return set_error(PA_ERR_ARG, "NULL buffer");
+  if (k >= n) return set_error(PA_ERR_ARG, "k = %zu is not below n = %zu", k, n);
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t stream = stream_of(opts);
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+  const bool in_dev = is_device_ptr(a);
+  const bool out_dev = is_device_ptr(out);
+  // Candidates kept after the first digit: a quarter of the input covers
+  // uniform and presorted inputs after one step; heavier bins are filtered
+  // from the input instead.
+  const size_t cand_cap = n / 4 + 1024;
+  const void* d_in = nullptr;
+  void *cand = nullptr, *work = nullptr, *d_out = nullptr;
+  auto layout = [&](Carve& c) {
+    d_in = in_dev ? a : c.take<char>(n * kb);
+    cand = c.take<char>(cand_cap * kb);
+    work = c.take<char>(select_state_bytes());
+    d_out = out_dev ? out : c.take<char>(8);
+  };
+  Carve m{nullptr};
+  layout(m);
+  if (int rc = ensure_dev(ws, stream, m.off)) return rc;
+  Carve r{ws->dev};
+  layout(r);
+  if (!in_dev) PA_CUDA(cudaMemcpyAsync(const_cast<void*>(d_in), a, n * kb, cudaMemcpyHostToDevice, stream));
+  PA_CUDA(launch_select(d_in, n, k, kb, cand, cand_cap, work, d_out, ws->err, stream));
+  if (!out_dev) PA_CUDA(cudaMemcpyAsync(out, d_out, kb, cudaMemcpyDeviceToHost, stream));
+  return finish(ws, stream, opts && opts->async_device && in_dev && out_dev);
+}
+
+// ---------------------------------------------------------------------------
+// Sum
+// ---------------------------------------------------------------------------
+int sum_impl(const void* a, size_t n, int kb, uint64_t* out, const pa_opts* opts) {
+  if (int rc = check_opts(opts)) return rc;
+  if (!out) return set_error(PA_ERR_ARG, "out is NULL");
+  if (n && !a) return set_error(PA_ERR_ARG, "input is NULL");
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t stream = stream_of(opts);
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+  const bool in_dev = is_device_ptr(a);
+  const bool out_dev = is_device_ptr(out);
+  const void* d_in = nullptr;
+  unsigned long long* partials = nullptr;
+  uint32_t* ticket = nullptr;
+  unsigned long long* d_out = nullptr;
+  auto layout = [&](Carve& c) {
+    d_in = in_dev ? a : c.take<char>(n * kb);
+    partials = c.take<unsigned long long>(sum_partials_needed());
+    ticket = c.take<uint32_t>(1);
+    d_out = out_dev ? reinterpret_cast<unsigned long long*>(out) : c.take<unsigned long long>(1);
+  };
+  Carve m{nullptr};
+  layout(m);
+  if (int rc = ensure_dev(ws, stream, m.off)) return rc;
+  Carve r{ws->dev};
+  layout(r);
+  if (!in_dev && n) PA_CUDA(cudaMemcpyAsync(const_cast<void*>(d_in), a, n * kb, cudaMemcpyHostToDevice, stream));
+  PA_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream));
+  PA_CUDA(launch_sum(d_in, n, kb, partials, ticket, d_out, stream));
+  if (!out_dev) PA_CUDA(cudaMemcpyAsync(out, d_out, sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+  return finish(ws, stream, opts && opts->async_device && in_dev && out_dev);
+}
+
+}  // namespace
+
+const DeviceInfo& device_info() {
+  static DeviceInfo infos[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  DeviceInfo& d = infos[dev];
+  if (d.device != dev) {
+    int sms = 0, smem = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    d.sm_count = sms > 0 ? sms : 1;
+    d.max_smem_optin = (size_t)smem;
+    d.device = dev;
+  }
+  return d;
+}
+
+}  // namespace pa
+
+using namespace pa;
+
+extern "C" {
+
+const char* pa_status_string(int status) {
+  switch (status) {
+    case PA_OK: return "PA_OK";
+    case PA_ERR_ARG: return "PA_ERR_ARG";
+    case PA_ERR_OOM: return "PA_ERR_OOM";
+    case PA_ERR_CUDA: return "PA_ERR_CUDA";
+    case PA_ERR_TIMEOUT: return "PA_ERR_TIMEOUT";
+    case PA_ERR_NO_DEVICE: return "PA_ERR_NO_DEVICE";
+    default: return "PA_ERR_UNKNOWN";
+  }
+}
+
+const char* pa_last_error_message(void) { return g_last_error.c_str(); }
+
+int pa_device_available(void) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return count > 0 ? 1 : 0;
+}
+
+int pa_stream_check(void* stream) {
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(static_cast<cudaStream_t>(stream), &ws)) return rc;
+  return finish(ws, static_cast<cudaStream_t>(stream), false);
+}
+
+int pa_release_workspaces(void) {
+  if (!pa_device_available()) return PA_OK;
+  std::lock_guard<std::mutex> lock(g_mu);
+  int dev0 = 0;
+  cudaGetDevice(&dev0);
+  for (auto& kv : g_ws) {
+    cudaSetDevice(kv.first.first);
+    cudaStreamSynchronize(kv.first.second);
+    if (kv.second.dev) cudaFree(kv.second.dev);
+    if (kv.second.err) cudaFree(kv.second.err);
+    if (kv.second.err_host) cudaFreeHost(kv.second.err_host);
+  }
+  g_ws.clear();
+  cudaSetDevice(dev0);
+  return PA_OK;
+}
+
+int pa_sort_u32(uint32_t* keys, uint32_t* tmp, size_t n, const pa_opts* opts) {
+  return sort_impl(keys, tmp, nullptr, nullptr, n, 4, false, opts);
+}
+int pa_sort_timed(int key_kind, void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t n,
+                  float* phase_ms, int phase_cap, const pa_opts* opts) {
+  if (!phase_ms || phase_cap <= 0) return set_error(PA_ERR_ARG, "phase_ms is required");
+  switch (key_kind) {
+    case PA_KEY_U32: return sort_impl(keys, tmp, vals, tmp_vals, n, 4, false, opts, phase_ms, phase_cap);
+    case PA_KEY_U64: return sort_impl(keys, tmp, vals, tmp_vals, n, 8, false, opts, phase_ms, phase_cap);
+    case PA_KEY_F32: return sort_impl(keys, tmp, vals, tmp_vals, n, 4, true, opts, phase_ms, phase_cap);
+    default: return set_error(PA_ERR_ARG, "unknown key kind %d", key_kind);
+  }
+}
+
+int pa_sort_u64(uint64_t* keys, uint64_t* tmp, size_t n, const pa_opts* opts) {
+  return sort_impl(keys, tmp, nullptr, nullptr, n, 8, false, opts);
+}
+int pa_sort_f32(float* keys, float* tmp, size_t n, const pa_opts* opts) {
+  return sort_impl(keys, tmp, nullptr, nullptr, n, 4, true, opts);
+}
+int pa_sort_kv_u32(uint32_t* keys, uint32_t* vals, uint32_t* tmp_keys, uint32_t* tmp_vals, size_t n,
+                   const pa_opts* opts) {
+  if (n && !vals) return set_error(PA_ERR_ARG, "vals is NULL");
+  return sort_impl(keys, tmp_keys, vals, tmp_vals, n, 4, false, opts);
+}
+int pa_sort_kv_u64(uint64_t* keys, uint32_t* vals, uint64_t* tmp_keys, uint32_t* tmp_vals, size_t n,
+                   const pa_opts* opts) {
+  if (n && !vals) return set_error(PA_ERR_ARG, "vals is NULL");
+  return sort_impl(keys, tmp_keys, vals, tmp_vals, n, 8, false, opts);
+}
+int pa_sort_kv_f32(float* keys, uint32_t* vals, float* tmp_keys, uint32_t* tmp_vals, size_t n,
+                   const pa_opts* opts) {
+  if (n && !vals) return set_error(PA_ERR_ARG, "vals is NULL");
+  return sort_impl(keys, tmp_keys, vals, tmp_vals, n, 4, true, opts);
+}
+
+int pa_sort_two_phase_u32(uint32_t* a, uint32_t* b, size_t n, const pa_opts* opts) {
+  if (n && !b) return set_error(PA_ERR_ARG, "b is NULL");
+  int rc = sort_impl(a, b, nullptr, nullptr, n, 4, false, opts);
+  if (rc != PA_OK || n == 0) return rc;
+  cudaStream_t stream = stream_of(opts);
+  PA_CUDA(cudaMemcpyAsync(b, a, n * sizeof(uint32_t), cudaMemcpyDefault, stream));
+  PA_CUDA(cudaStreamSynchronize(stream));
+  return PA_OK;
+}
+
+int pa_hist_byte_components_u32(const uint32_t* a, size_t n, uint64_t* out, const pa_opts* opts) {
+  return hist_impl(a, n, 4, 4, 0, 8, out, opts);
+}
+
+int pa_hist_one_byte_u32(const uint32_t* a, size_t n, unsigned shift, uint64_t* out, const pa_opts* opts) {
+  if (shift >= 32) return set_error(PA_ERR_ARG, "shift %u is not below 32", shift);
+  return hist_impl(a, n, 4, 1, shift, 0, out, opts);
+}
+
+int pa_hist_u8(const uint8_t* a, size_t n, uint64_t* out, const pa_opts* opts) {
+  return hist_impl(a, n, 1, 1, 0, 0, out, opts);
+}
+
+int pa_hist_quanta_u32(const uint32_t* a, size_t l, size_t r, size_t work_quanta, size_t quanta,
+                       unsigned which_byte, uint64_t* out, const pa_opts* opts) {
+  if (int rc = check_opts(opts)) return rc;
+  if (!out || (quanta && !a)) return set_error(PA_ERR_ARG, "NULL buffer");
+  if (which_byte > 3) return set_error(PA_ERR_ARG, "which_byte %u is not below 4", which_byte);
+  if (work_quanta == 0) return set_error(PA_ERR_ARG, "work_quanta is 0");
+  if (l <= r && r / work_quanta >= quanta)
+    return set_error(PA_ERR_ARG, "index %zu falls in quantum %zu, beyond quanta = %zu", r, r / work_quanta, quanta);
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t stream = stream_of(opts);
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+  const size_t len = l <= r ? r - l + 1 : 0;
+  const bool in_dev = is_device_ptr(a);
+  const bool out_dev = is_device_ptr(out);
+  const uint32_t* d_in = nullptr;
+  unsigned long long* d_out = nullptr;
+  auto layout = [&](Carve& c) {
+    d_in = in_dev ? a + l : c.take<uint32_t>(len);
+    d_out = out_dev ? reinterpret_cast<unsigned long long*>(out) : c.take<unsigned long long>(quanta * 256);
+  };
+  Carve m{nullptr};
+  layout(m);
+  if (int rc = ensure_dev(ws, stream, m.off)) return rc;
+  Carve rr{ws->dev};
+  layout(rr);
+  if (!in_dev && len)
+    PA_CUDA(cudaMemcpyAsync(const_cast<uint32_t*>(d_in), a + l, len * 4, cudaMemcpyHostToDevice, stream));
+  PA_CUDA(cudaMemsetAsync(d_out, 0, quanta * 256 * sizeof(uint64_t), stream));
+  if (len) PA_CUDA(launch_quanta_counts(d_in, l, l + len, work_quanta, which_byte, d_out, stream));
+  if (!out_dev) PA_CUDA(cudaMemcpyAsync(out, d_out, quanta * 256 * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+  return finish(ws, stream, opts && opts->async_device && in_dev && out_dev);
+}
+
+int pa_start_of_bins_u32(const uint32_t* a, size_t n, size_t work_quanta, size_t quanta, unsigned digit,
+                         uint64_t* out, const pa_opts* opts) {
+  if (int rc = check_opts(opts)) return rc;
+  if (!out || (n && !a)) return set_error(PA_ERR_ARG, "NULL buffer");
+  if (digit > 3) return set_error(PA_ERR_ARG, "digit %u is not below 4", digit);
+  if (work_quanta == 0) return set_error(PA_ERR_ARG, "work_quanta is 0");
+  if (n && (n - 1) / work_quanta >= quanta)
+    return set_error(PA_ERR_ARG, "n = %zu needs more than quanta = %zu", n, quanta);
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t stream = stream_of(opts);
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+  const bool in_dev = is_device_ptr(a);
+  const bool out_dev = is_device_ptr(out);
+  const uint32_t* d_in = nullptr;
+  unsigned long long *counts = nullptr, *sob = nullptr;
+  auto layout = [&](Carve& c) {
+    d_in = in_dev ? a : c.take<uint32_t>(n);
+    counts = c.take<unsigned long long>(quanta * 256);
+    sob = c.take<unsigned long long>(quanta * 256 + 256);
+  };
+  Carve m{nullptr};
+  layout(m);
+  if (int rc = ensure_dev(ws, stream, m.off)) return rc;
+  Carve rr{ws->dev};
+  layout(rr);
+  if (!in_dev && n) PA_CUDA(cudaMemcpyAsync(const_cast<uint32_t*>(d_in), a, n * 4, cudaMemcpyHostToDevice, stream));
+  PA_CUDA(cudaMemsetAsync(counts, 0, quanta * 256 * sizeof(uint64_t), stream));
+  if (n) PA_CUDA(launch_quanta_counts(d_in, 0, n, work_quanta, digit, counts, stream));
+  PA_CUDA(launch_quanta_start_of_bins(counts, quanta, sob, stream));
+  PA_CUDA(cudaMemcpyAsync(out, sob, quanta * 256 * sizeof(uint64_t), out_dev ? cudaMemcpyDeviceToDevice
+                                                                             : cudaMemcpyDeviceToHost,
+                          stream));
+  return finish(ws, stream, opts && opts->async_device && in_dev && out_dev);
+}
+
+int pa_select_u32(const uint32_t* a, size_t n, size_t k, uint32_t* out, const pa_opts* opts) {
+  return select_impl(a, n, k, 4, out, opts);
+}
+int pa_select_u64(const uint64_t* a, size_t n, size_t k, uint64_t* out, const pa_opts* opts) {
+  return select_impl(a, n, k, 8, out, opts);
+}
+
+int pa_select_radix_u32(uint32_t* a, size_t start, size_t length, size_t k, uint32_t* out, const pa_opts* opts) {
+  if (!a || !out) return set_error(PA_ERR_ARG, "NULL buffer");
+  if (length == 0 || k < start || k - start >= length)
+    return set_error(PA_ERR_ARG, "k = %zu is outside [start, start + length) = [%zu, %zu)", k, start, start + length);
+  uint32_t v = 0;
+  int rc = select_impl(a + start, length, k - start, 4, &v, opts);
+  if (rc != PA_OK) return rc;
+  cudaStream_t stream = stream_of(opts);
+  PA_CUDA(cudaMemcpyAsync(a + k, &v, sizeof(v), cudaMemcpyDefault, stream));
+  PA_CUDA(cudaMemcpyAsync(out, &v, sizeof(v), cudaMemcpyDefault, stream));
+  PA_CUDA(cudaStreamSynchronize(stream));
+  return PA_OK;
+}
+
+int pa_sum_u32(const uint32_t* a, size_t n, uint64_t* out, const pa_opts* opts) {
+  return sum_impl(a, n, 4, out, opts);
+}
+int pa_sum_u64(const uint64_t* a, size_t n, uint64_t* out, const pa_opts* opts) {
+  return sum_impl(a, n, 8, out, opts);
+}
+
+}  // extern "C"

@@ -1,0 +1,111 @@
+// Host-side launchers of the radix hot-path kernels.  Each launcher enqueues
+// work on `stream` and returns a cudaError_t from the launch; none of them
+// synchronises.  The C ABI (pa_capi.cu) owns workspace, pointer
+// classification and error reporting.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pa {
+
+constexpr int kMaxPasses = 8;  // 64-bit keys, 8-bit digits
+
+// Per-pass control computed on the device from the digit histograms, so the
+// host never waits for them: a pass whose digit puts every key in one bin is
+// the identity permutation and is skipped; the ping-pong direction and the
+// float transform (applied on the first executed pass's loads, undone on the
+// last executed pass's stores) follow from the passes that remain.
+struct PassCtrl {
+  uint32_t skip;
+  uint32_t src_is_tmp;
+  uint32_t transform_in;
+  uint32_t transform_out;
+};
+struct SortCtrl {
+  PassCtrl pass[kMaxPasses];
+  uint32_t final_in_tmp;
+  uint32_t executed;
+};
+
+// Device properties the launchers size grids with (filled once per device).
+struct DeviceInfo {
+  int device = -1;
+  int sm_count = 0;
+  size_t max_smem_optin = 0;
+};
+const DeviceInfo& device_info();
+
+// ---- histograms (pa_histogram.cu) -----------------------------------------
+// Counts of `num_digits` digits of width `radix_bits` (digit d taken at bit
+// shift0 + d * shift_step of the ordered key) over keys[0, n), ADDED into
+// out[num_digits][1 << radix_bits] (unsigned 64-bit).  key_bytes is 1, 4 or 8.
+cudaError_t launch_digit_counts(const void* keys, size_t n, int key_bytes, int num_digits, int radix_bits,
+                                uint32_t shift0, uint32_t shift_step, bool is_float, unsigned long long* out,
+                                cudaStream_t stream);
+
+// Counts of byte `which_byte` of the keys with absolute index in [l, r)
+// (keys points at index l), per work quantum (quantum = index / work_quanta),
+// ADDED into out[quantum][256].
+cudaError_t launch_quanta_counts(const uint32_t* keys, size_t l, size_t r, size_t work_quanta,
+                                 uint32_t which_byte, unsigned long long* out, cudaStream_t stream);
+
+// start_of_bins[q][b] = sum of all bins < b over all quanta + sum of bin b over
+// quanta < q, from counts[q][256] (RadixSortLsdParallel.h:128-156 on device).
+// start_of_bins must hold quanta * 256 + 256 words (the tail holds bin totals).
+cudaError_t launch_quanta_start_of_bins(const unsigned long long* counts, size_t quanta,
+                                        unsigned long long* start_of_bins, cudaStream_t stream);
+
+// Exclusive scan of each pass's digit counts into bin_start, and the pass
+// control block (skips, ping-pong direction, float transform placement).
+cudaError_t launch_scan_digits(const unsigned long long* counts, int passes, int radix_bits, size_t n,
+                               bool is_float, bool allow_skip, unsigned long long* bin_start, SortCtrl* ctrl,
+                               cudaStream_t stream);
+
+// ---- onesweep digit pass (pa_onesweep.cu) --------------------------------
+struct OnesweepArgs {
+  void* keys_a;  // the caller's key buffer
+  void* keys_b;  // the scratch key buffer
+  uint32_t* vals_a;
+  uint32_t* vals_b;
+  size_t n;
+  uint32_t shift;
+  int pass;
+  int is_float;
+  const unsigned long long* bin_start;  // this pass's 256 exclusive bin starts
+  void* status;                         // this pass's tiles * 256 look-back words
+  uint32_t* tile_counter;               // this pass's tile ticket
+  const SortCtrl* ctrl;
+  uint32_t* err;
+};
+
+// Tile geometry chosen for (key_bytes, has_vals); the workspace is sized
+// with it.
+size_t onesweep_tile_keys(int key_bytes, bool has_vals);
+// Bytes of one look-back status word for n keys (4 when n < 2^30, else 8).
+size_t onesweep_status_bytes(size_t n);
+cudaError_t launch_onesweep_pass(const OnesweepArgs& a, int key_bytes, bool has_vals, cudaStream_t stream);
+
+// Copies the result back into the caller's buffers when the executed passes
+// left it in the scratch buffers (device-side decision from SortCtrl).
+cudaError_t launch_final_copy(void* keys_a, const void* keys_b, uint32_t* vals_a, const uint32_t* vals_b,
+                              size_t n, int key_bytes, const SortCtrl* ctrl, cudaStream_t stream);
+
+// ---- sum (pa_sum.cu) -------------------------------------------------------
+// out = sum of keys[0, n) modulo 2^64.  partials holds sum_partials_needed()
+// words and ticket one zeroed word.
+size_t sum_partials_needed();
+cudaError_t launch_sum(const void* keys, size_t n, int key_bytes, unsigned long long* partials, uint32_t* ticket,
+                       unsigned long long* out, cudaStream_t stream);
+
+// ---- select (pa_select.cu) -------------------------------------------------
+struct SelectState;
+size_t select_state_bytes();
+// k-th smallest (0-based) of keys[0, n) into *out (device).  cand holds
+// cand_cap keys; work is select_state_bytes() of scratch (initialised by the
+// launcher).
+cudaError_t launch_select(const void* keys, size_t n, size_t k, int key_bytes, void* cand, size_t cand_cap,
+                          void* work, void* out, uint32_t* err, cudaStream_t stream);
+
+}  // namespace pa

@@ -1,0 +1,78 @@
+// A C++ caller of the reference's radix entry points, switched to the GPU by
+// changing only the include path (-I include/ParallelAlgorithms) and linking
+// libpa_gb300.so.  Self-checking in the style of the reference's benchmarks
+// (RadixSortLsdBenchmark.cpp:78-114, RadixSelectBenchmark.cpp:33-69,
+// SumBenchmark.cpp:116-163): each result is compared with the standard
+// library and a mismatch exits non-zero.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <numeric>
+#include <random>
+#include <vector>
+
+#include "RadixSortLsdParallel.h"
+#include "HistogramParallel.h"
+#include "RadixSelect.h"
+#include "SumParallel.h"
+
+static int fail(const char* what) {
+  std::printf("FAIL: %s\n", what);
+  return 1;
+}
+
+int main(int argc, char** argv) {
+  const size_t n = argc > 1 ? std::strtoull(argv[1], nullptr, 10) : 1000003;
+  std::mt19937_64 dist(1234);
+  std::vector<unsigned> uints(n);
+  for (auto& d : uints) d = static_cast<unsigned>(dist());
+
+  // SortRadixPar(a, tmp, n) vs std::stable_sort
+  std::vector<unsigned> a(uints), tmp(n), ref(uints);
+  std::stable_sort(ref.begin(), ref.end());
+  ParallelAlgorithms::SortRadixPar(a.data(), tmp.data(), n);
+  if (a != ref) return fail("SortRadixPar(a, tmp, n)");
+  std::vector<unsigned> a2(uints);
+  ParallelAlgorithms::SortRadixPar(a2.data(), n);
+  if (a2 != ref) return fail("SortRadixPar(a, n)");
+  std::vector<unsigned> a3(uints), b3(n);
+  ParallelAlgorithms::RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase(a3.data(), b3.data(), n);
+  if (a3 != ref || b3 != ref) return fail("RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase");
+
+  // HistogramByteComponentsParallel<256,8>: 8 rows, rows 4-7 zero
+  size_t** h = ParallelAlgorithms::HistogramByteComponentsParallel<256, 8>(uints.data(), 0, n - 1);
+  for (unsigned d = 0; d < 8; ++d) {
+    std::vector<size_t> c(256, 0);
+    if (d < 4)
+      for (unsigned v : uints) c[(v >> (8 * d)) & 255]++;
+    for (int b = 0; b < 256; ++b)
+      if (h[d][b] != c[b]) return fail("HistogramByteComponentsParallel");
+    delete[] h[d];
+  }
+  delete[] h;
+  size_t* h1 = ParallelAlgorithms::HistogramOneByteComponentParallel<256, 8>(uints.data(), 0, n - 1, 13);
+  {
+    std::vector<size_t> c(256, 0);
+    for (unsigned v : uints) c[(v >> 13) & 255]++;
+    for (int b = 0; b < 256; ++b)
+      if (h1[b] != c[b]) return fail("HistogramOneByteComponentParallel");
+  }
+  delete[] h1;
+
+  // SelectRadix(a, n, k) vs std::nth_element, k = n - 21 as the reference benchmark
+  if (n > 21) {
+    const size_t k = n - 21;
+    std::vector<unsigned> s(uints), nth(uints);
+    std::nth_element(nth.begin(), nth.begin() + k, nth.end());
+    unsigned v = SelectRadix(s.data(), n, k);
+    if (v != nth[k] || s[k] != nth[k]) return fail("SelectRadix");
+  }
+
+  // SumParallelNonRecursive vs std::accumulate
+  const unsigned long long sref = std::accumulate(uints.begin(), uints.end(), 0ULL);
+  if (ParallelAlgorithms::SumParallelNonRecursive(uints.data(), 0, n) != sref) return fail("SumParallelNonRecursive");
+  if ((unsigned long long)ParallelAlgorithms::SumParallel(uints.data(), 0, n) != sref) return fail("SumParallel");
+
+  std::printf("OK n=%zu\n", n);
+  return 0;
+}

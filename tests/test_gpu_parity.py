@@ -1,0 +1,227 @@
+"""GPU path vs the CPU oracle, bit-exact, through the C ABI.
+
+Inputs are seeded and sized so the oracle finishes in seconds; sizes sit on
+both sides of every tile boundary the kernels use (8192 keys for 32-bit
+keys, 6144 for 32-bit key+payload and 64-bit keys, 4096 for 64-bit
+key+payload) and below the reference's insertion-sort cutoff (100).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [1, 2, 7, 99, 100, 101, 1000, 4095, 4096, 4097, 6143, 6144, 6145, 8191, 8192, 8193, 16385, 65536,
+         100003, 1 << 20, 3_000_017]
+
+
+def u32_inputs(n: int) -> dict[str, np.ndarray]:
+    from parallelalgorithms_gb300 import workloads
+    rng = np.random.default_rng(n)
+    nearly = np.arange(n, dtype=np.uint32)
+    nearly[::100] = 0x1010
+    return {
+        "uniform": workloads.uniform_u32(n),
+        "presorted": np.arange(n, dtype=np.uint32),
+        "descending": np.arange(n, dtype=np.uint32)[::-1].copy(),
+        "constant": np.full(n, 42, np.uint32),
+        "nearly": nearly,
+        "few": rng.integers(0, 16, n, dtype=np.uint32),
+        "high_byte": (rng.integers(0, 256, n, dtype=np.uint32) << np.uint32(24)),
+        "max": np.full(n, 0xFFFFFFFF, np.uint32),
+    }
+
+
+def to_dev(torch, a: np.ndarray):
+    view = {np.dtype(np.uint32): np.int32, np.dtype(np.uint64): np.int64, np.dtype(np.float32): np.float32,
+            np.dtype(np.uint8): np.uint8}[a.dtype]
+    return torch.from_numpy(a.view(view).copy()).cuda()
+
+
+def from_dev(t, dtype) -> np.ndarray:
+    return t.cpu().numpy().view(dtype)
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_sort_u32_host_and_device_match_oracle(pa, port, torch_cuda, n):
+    for name, a in u32_inputs(n).items():
+        want, _ = port.sort(a)
+        h = a.copy()
+        pa.SortRadixPar(h, np.empty_like(h), n)
+        np.testing.assert_array_equal(h, want, err_msg=f"host {name} n={n}")
+        d = to_dev(torch_cuda, a)
+        pa.sort(d)
+        torch_cuda.cuda.synchronize()
+        np.testing.assert_array_equal(from_dev(d, np.uint32), want, err_msg=f"device {name} n={n}")
+
+
+@pytest.mark.parametrize("n", [1, 100, 4097, 6144, 6145, 65537, 1 << 20])
+def test_sort_kv_u32_stable(pa, port, n):
+    for name, a in u32_inputs(n).items():
+        vals = np.arange(n, dtype=np.uint32)
+        wk, wv = port.sort(a, vals)
+        k, v = a.copy(), vals.copy()
+        pa.sort(k, v)
+        np.testing.assert_array_equal(k, wk, err_msg=name)
+        np.testing.assert_array_equal(v, wv, err_msg=name)
+
+
+@pytest.mark.parametrize("n", [1, 99, 4096, 6143, 6144, 6145, 100003, 1 << 20])
+def test_sort_u64_and_kv_u64(pa, port, n):
+    from parallelalgorithms_gb300 import workloads
+    rng = np.random.default_rng(7 + n)
+    cases = {
+        "uniform": workloads.uniform_u64(n),
+        "zipf": workloads.zipf_u64(n),
+        "top_byte": rng.integers(0, 256, n, dtype=np.uint64) << np.uint64(56),
+        "constant": np.full(n, 0xDEADBEEFCAFEF00D, np.uint64),
+        "small": rng.integers(0, 1000, n, dtype=np.uint64),
+    }
+    for name, a in cases.items():
+        want, _ = port.sort(a)
+        k = a.copy()
+        pa.sort(k)
+        np.testing.assert_array_equal(k, want, err_msg=name)
+        vals = np.arange(n, dtype=np.uint32)
+        wk, wv = port.sort(a, vals)
+        k, v = a.copy(), vals.copy()
+        pa.sort(k, v)
+        np.testing.assert_array_equal(k, wk, err_msg=name)
+        np.testing.assert_array_equal(v, wv, err_msg=name)
+
+
+@pytest.mark.parametrize("n", [1, 2, 100, 8193, 100003, 1 << 20])
+def test_sort_f32_total_order_and_payload(pa, port, torch_cuda, n):
+    from parallelalgorithms_gb300 import workloads
+    a = workloads.normal_specials_f32(n)
+    want, _ = port.sort(a)
+    k = a.copy()
+    pa.sort(k)
+    np.testing.assert_array_equal(k.view(np.uint32), want.view(np.uint32))
+    vals = np.arange(n, dtype=np.uint32)
+    wk, wv = port.sort(a, vals)
+    k, v = a.copy(), vals.copy()
+    pa.sort(k, v)
+    np.testing.assert_array_equal(k.view(np.uint32), wk.view(np.uint32))
+    np.testing.assert_array_equal(v, wv)
+    d = to_dev(torch_cuda, a)
+    pa.sort(d)
+    np.testing.assert_array_equal(from_dev(d, np.float32).view(np.uint32), want.view(np.uint32))
+
+
+def test_sort_f32_all_equal_digits_skips_passes(pa, port):
+    # constant float keys: every pass is trivial, the transform must not leak
+    for v in (-0.0, 0.0, -1.5, np.inf):
+        a = np.full(10001, v, np.float32)
+        k = a.copy()
+        pa.sort(k)
+        np.testing.assert_array_equal(k.view(np.uint32), a.view(np.uint32))
+    # one non-trivial pass only (low byte differs), negative numbers
+    base = np.float32(-1.0).view(np.uint32)
+    a = (base + np.random.default_rng(1).integers(0, 200, 50000, dtype=np.uint32)).view(np.float32)
+    want, _ = port.sort(a)
+    k = a.copy()
+    pa.sort(k)
+    np.testing.assert_array_equal(k.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [1, 99, 8192, 8193, 100003, 1 << 20])
+def test_histograms_match_oracle(pa, port, n):
+    for name, a in u32_inputs(n).items():
+        np.testing.assert_array_equal(pa.HistogramByteComponentsParallel(a, 0, n - 1),
+                                      port.hist_byte_components(a, 0, n - 1), err_msg=name)
+        for sh in (0, 5, 8, 16, 24, 31):
+            np.testing.assert_array_equal(pa.HistogramOneByteComponentParallel(a, 0, n - 1, sh),
+                                          port.hist_one_byte(a, 0, n - 1, sh), err_msg=f"{name} shift {sh}")
+        if n > 10:
+            l, r = 3, n - 5
+            np.testing.assert_array_equal(pa.HistogramByteComponentsParallel(a, l, r),
+                                          port.hist_byte_components(a, l, r), err_msg=name)
+        u8 = (a & np.uint32(0xFF)).astype(np.uint8)
+        np.testing.assert_array_equal(pa.HistogramOneByteComponentParallel(u8, 0, n), port.hist_u8(u8, 0, n))
+        if n > 20:
+            np.testing.assert_array_equal(pa.HistogramOneByteComponentParallel(u8, 7, n - 3),
+                                          port.hist_u8(u8, 7, n - 3))
+
+
+@pytest.mark.parametrize("n", [1, 1000, 100003])
+def test_quanta_histogram_and_start_of_bins(pa, port, n):
+    a = u32_inputs(n)["uniform"]
+    for wq in (1, 7, 4096, max(1, n // 3), n):
+        q = (n - 1) // wq + 1
+        for byte in range(4):
+            np.testing.assert_array_equal(pa.HistogramByteComponentsQCPar(a, 0, n - 1, wq, q, byte),
+                                          port.hist_qc(a, 0, n - 1, wq, q, byte))
+            np.testing.assert_array_equal(pa.ComputeStartOfBinsPar(a, n, wq, q, byte),
+                                          port.start_of_bins(a, n, wq, q, byte))
+        if n > 10:
+            np.testing.assert_array_equal(pa.HistogramByteComponentsQCPar(a, 2, n - 3, wq, q, 1),
+                                          port.hist_qc(a, 2, n - 3, wq, q, 1))
+
+
+@pytest.mark.parametrize("n", [1, 2, 99, 100, 8193, 100003, 1 << 20, 3_000_017])
+def test_select_matches_oracle(pa, port, n):
+    for name, a in u32_inputs(n).items():
+        for k in sorted({0, n // 2, max(0, n - 21), n - 1}):
+            want = port.select(a, k)
+            assert pa.select(a, k) == want, (name, k)
+            c = a.copy()
+            assert pa.SelectRadix(c, n, k) == want
+            assert c[k] == want  # the reference leaves the k-th element at a[k]
+    if n > 100:
+        a = u32_inputs(n)["uniform"]
+        start, length = 17, n - 40
+        k = start + length // 3
+        assert pa.SelectRadix(a.copy(), start, length, k) == port.select(a, k, start=start, length=length)
+
+
+@pytest.mark.parametrize("n", [1, 99, 100003, 1 << 20])
+def test_select_u64(pa, port, n):
+    from parallelalgorithms_gb300 import workloads
+    for a in (workloads.uniform_u64(n), workloads.zipf_u64(n), np.full(n, 7, np.uint64)):
+        for k in sorted({0, n // 3, n - 1}):
+            assert pa.select(a, k) == port.select(a, k)
+
+
+@pytest.mark.parametrize("n", [0, 1, 3, 4, 5, 17, 100003, 1 << 20, 3_000_017])
+def test_sum_matches_oracle(pa, port, torch_cuda, n):
+    a = u32_inputs(max(n, 1))["uniform"][:n]
+    assert pa.SumParallelNonRecursive(a, 0, n) == port.sum(a)
+    m = np.full(n, 0xFFFFFFFF, np.uint32)
+    assert pa.SumParallelNonRecursive(m, 0, n) == port.sum(m)
+    w = np.full(n, 0xFFFFFFFFFFFFFFFF, np.uint64)  # wraps modulo 2^64
+    assert pa.SumParallel(w, 0, n) == port.sum(w)
+    if n > 10:
+        assert pa.SumParallelNonRecursive(a, 3, n - 2) == port.sum(a, 3, n - 2)
+        s = pa.SumParallel(a, 0, n)
+        assert s == np.int64(np.uint64(port.sum(a)))
+        d = to_dev(torch_cuda, a)
+        assert pa.sum_u64(d) == port.sum(a)
+        assert pa.sum_u64(d[1:]) == port.sum(a, 1, n)  # unaligned start
+
+
+def test_two_phase_leaves_result_in_both(pa, port):
+    a = u32_inputs(50001)["uniform"]
+    want, _ = port.sort(a)
+    x, b = a.copy(), np.zeros_like(a)
+    pa.RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase(x, b, a.size)
+    np.testing.assert_array_equal(x, want)
+    np.testing.assert_array_equal(b, want)
+
+
+def test_unaligned_device_buffers(pa, port, torch_cuda):
+    # tiles of a buffer that does not start on 16 bytes take the plain-load path
+    a = u32_inputs(100003)["uniform"]
+    want, _ = port.sort(a[1:])
+    base = to_dev(torch_cuda, a)
+    view = base[1:]
+    pa.sort(view)
+    np.testing.assert_array_equal(from_dev(view, np.uint32), want)
+
+
+def test_repeated_calls_reuse_workspace(pa, port):
+    for n in (100003, 5, 1 << 20, 100003, 3):
+        a = u32_inputs(n)["uniform"]
+        want, _ = port.sort(a)
+        k = a.copy()
+        pa.sort(k)
+        np.testing.assert_array_equal(k, want)
