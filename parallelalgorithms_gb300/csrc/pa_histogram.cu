@@ -7,49 +7,57 @@
 // arbitrary shift is HistogramOneByteComponentParallel (:535-576), and with
 // 1-byte keys the unsigned-char overloads (:16-247).
 //
-// Each CTA keeps num_digits x 2^radix_bits u32 counters in shared memory,
-// streams a grid-strided share of the keys with 16-byte loads, and adds its
-// counters into the 64-bit global result once at the end.  When all 32
-// lanes of a warp hold the same digit (constant or presorted runs) the warp
-// makes one shared atomic of 32 instead of 32 colliding ones.
+// Each CTA keeps its counters in shared memory "lane-banked": counter
+// (digit d, bin b) is replicated once per lane, at word (d * 2^radix_bits + b)
+// * LANES + lane % LANES, so the 32 atomics of a warp-wide update always land
+// in distinct banks whatever the key distribution (constant input included).
+// A CTA streams a grid-strided share of the keys with 16-byte loads, then
+// folds the lane copies and adds its counts into the 64-bit global result.
 #include "pa_common.cuh"
 #include "pa_kernels.cuh"
 
 namespace pa {
 namespace {
 
-constexpr int kHistBlock = 512;
-
-template <typename K, int ND, int RB>
-__device__ __forceinline__ void count_key(uint32_t* s_hist, K key, bool valid, uint32_t shift0, uint32_t step) {
-  constexpr uint32_t R = 1u << RB;
-  constexpr uint32_t FULL = 0xFFFFFFFFu;
-  const uint32_t vmask = __ballot_sync(FULL, valid);
-#pragma unroll
-  for (int d = 0; d < ND; ++d) {
-    const uint32_t b = valid ? (uint32_t)(key >> (shift0 + (uint32_t)d * step)) & (R - 1) : 0u;
-    const uint32_t b0 = __shfl_sync(FULL, b, __ffs(vmask) - 1);
-    if (__all_sync(FULL, !valid || b == b0)) {
-      if ((threadIdx.x & 31u) == 0 && vmask) atomicAdd(&s_hist[d * R + b0], (uint32_t)__popc(vmask));
-    } else if (valid) {
-      atomicAdd(&s_hist[d * R + b], 1u);
-    }
-  }
-}
+constexpr int kHistBlock = 1024;
 
 // Keys per 16-byte vector.
 template <typename K>
 constexpr int kVec = 16 / (int)sizeof(K);
 
+// Lane copies per counter: 32 (one bank per lane) while the table fits the
+// 227 KB of shared memory, else 16.
+template <int ND, int RB>
+constexpr int kLanes = (ND * (1 << RB) * 32 * 4 <= 160 * 1024) ? 32 : 16;
+
+template <int ND, int RB>
+constexpr size_t hist_smem_bytes() {
+  return (size_t)ND * (1 << RB) * kLanes<ND, RB> * 4;
+}
+
 template <typename K, int ND, int RB>
-__global__ void __launch_bounds__(kHistBlock) digit_counts_kernel(const K* __restrict__ keys, size_t n,
-                                                                    uint32_t shift0, uint32_t step, int is_float,
-                                                                    unsigned long long* __restrict__ out) {
+__global__ void __launch_bounds__(kHistBlock, 1) digit_counts_kernel(const K* __restrict__ keys, size_t n,
+                                                                       uint32_t shift0, uint32_t step, int is_float,
+                                                                       unsigned long long* __restrict__ out) {
   constexpr int R = 1 << RB;
   constexpr int V = kVec<K>;
-  __shared__ uint32_t s_hist[ND * R];
-  for (int i = threadIdx.x; i < ND * R; i += kHistBlock) s_hist[i] = 0;
+  constexpr int L = kLanes<ND, RB>;
+  constexpr uint32_t kWords = (uint32_t)ND * R * L;
+  extern __shared__ uint32_t s_h[];
+  for (uint32_t i = threadIdx.x; i < kWords; i += kHistBlock) s_h[i] = 0;
   __syncthreads();
+  const uint32_t lane = threadIdx.x % L;
+  uint32_t* my = s_h + lane;
+  const bool flt = is_float != 0;
+
+  auto count = [&](K key) {
+    if (sizeof(K) == 4) key = to_ordered(key, flt);
+#pragma unroll
+    for (int d = 0; d < ND; ++d) {
+      const uint32_t b = (uint32_t)(key >> (shift0 + (uint32_t)d * step)) & (R - 1);
+      atomicAdd(my + ((uint32_t)d * R + b) * L, 1u);
+    }
+  };
 
   // Split [0, n) into an unaligned head, whole 16-byte vectors, and a tail.
   const uintptr_t addr = reinterpret_cast<uintptr_t>(keys);
@@ -58,41 +66,36 @@ __global__ void __launch_bounds__(kHistBlock) digit_counts_kernel(const K* __res
   const size_t nvec = (n - head) / V;
   const size_t tail_start = head + nvec * V;
   const uint4* vec = reinterpret_cast<const uint4*>(keys + head);
-
-  const size_t warps_total = (size_t)gridDim.x * (kHistBlock / 32);
-  const size_t gwarp = (size_t)blockIdx.x * (kHistBlock / 32) + (threadIdx.x >> 5);
-  const uint32_t lane = threadIdx.x & 31u;
-  // Warp-uniform trip count: every lane of a warp runs the same iterations,
-  // so the warp-wide votes in count_key see all 32 lanes.
-  for (size_t w = gwarp; w * 32 < nvec; w += warps_total) {
-    const size_t vi = w * 32 + lane;
-    const bool valid = vi < nvec;
-    uint4 q = make_uint4(0, 0, 0, 0);
-    if (valid) q = ld_stream_v4(vec + vi);
-    const K* ks = reinterpret_cast<const K*>(&q);
+  const size_t stride = (size_t)gridDim.x * kHistBlock;
+  size_t i = (size_t)blockIdx.x * kHistBlock + threadIdx.x;
+  for (; i + stride < nvec; i += 2 * stride) {  // two 16-byte loads in flight
+    const uint4 q0 = ld_stream_v4(vec + i);
+    const uint4 q1 = ld_stream_v4(vec + i + stride);
+    const K* k0 = reinterpret_cast<const K*>(&q0);
+    const K* k1 = reinterpret_cast<const K*>(&q1);
 #pragma unroll
-    for (int e = 0; e < V; ++e) {
-      K key = ks[e];
-      if (sizeof(K) == 4) key = to_ordered(key, is_float != 0);
-      count_key<K, ND, RB>(s_hist, key, valid, shift0, step);
-    }
+    for (int e = 0; e < V; ++e) count(k0[e]);
+#pragma unroll
+    for (int e = 0; e < V; ++e) count(k1[e]);
   }
-  // Head and tail (fewer than 2 * V keys in total) go to the first warp.
-  if (blockIdx.x == 0 && threadIdx.x < 32) {
+  for (; i < nvec; i += stride) {
+    const uint4 q0 = ld_stream_v4(vec + i);
+    const K* k0 = reinterpret_cast<const K*>(&q0);
+#pragma unroll
+    for (int e = 0; e < V; ++e) count(k0[e]);
+  }
+  if (blockIdx.x == 0) {  // head and tail: fewer than 2 * V keys
     const size_t rest = head + (n - tail_start);
-    for (size_t base = 0; base < rest; base += 32) {
-      const size_t r = base + lane;
-      const bool valid = r < rest;
-      K key = 0;
-      if (valid) key = keys[r < head ? r : tail_start + (r - head)];
-      if (sizeof(K) == 4) key = to_ordered(key, is_float != 0);
-      count_key<K, ND, RB>(s_hist, key, valid, shift0, step);
-    }
+    for (size_t r = threadIdx.x; r < rest; r += kHistBlock) count(keys[r < head ? r : tail_start + (r - head)]);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < ND * R; i += kHistBlock) {
-    const uint32_t c = s_hist[i];
-    if (c) atomicAdd(&out[i], (unsigned long long)c);
+  // Fold the lane copies: thread e sums counter e's L copies, starting at a
+  // lane-dependent copy so that a warp's reads hit distinct banks.
+  for (uint32_t e = threadIdx.x; e < (uint32_t)(ND * R); e += kHistBlock) {
+    uint32_t sum = 0;
+#pragma unroll 8
+    for (int j = 0; j < L; ++j) sum += s_h[e * L + ((j + e) % L)];
+    if (sum) atomicAdd(&out[e], (unsigned long long)sum);
   }
 }
 
@@ -100,13 +103,19 @@ template <typename K, int ND, int RB>
 cudaError_t launch_counts_t(const void* keys, size_t n, uint32_t shift0, uint32_t step, bool is_float,
                             unsigned long long* out, cudaStream_t stream) {
   constexpr int V = kVec<K>;
-  const size_t work_warps = ceil_div(ceil_div(n, (size_t)V), (size_t)32 * 8);
-  const size_t max_blocks = (size_t)device_info().sm_count * 4;
-  size_t blocks = ceil_div(work_warps, (size_t)(kHistBlock / 32));
-  if (blocks > max_blocks) blocks = max_blocks;
+  auto kern = digit_counts_kernel<K, ND, RB>;
+  constexpr size_t smem = hist_smem_bytes<ND, RB>();
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  const size_t work = ceil_div(ceil_div(n, (size_t)V), (size_t)kHistBlock * 4);
+  size_t blocks = work < (size_t)device_info().sm_count ? work : (size_t)device_info().sm_count;
   if (blocks < 1) blocks = 1;
-  digit_counts_kernel<K, ND, RB><<<(unsigned)blocks, kHistBlock, 0, stream>>>(static_cast<const K*>(keys), n, shift0,
-                                                                             step, is_float ? 1 : 0, out);
+  kern<<<(unsigned)blocks, kHistBlock, smem, stream>>>(static_cast<const K*>(keys), n, shift0, step,
+                                                       is_float ? 1 : 0, out);
   return cudaGetLastError();
 }
 

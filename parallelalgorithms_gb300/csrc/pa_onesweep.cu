@@ -6,27 +6,31 @@
 // (ComputeStartOfBinsPar, :108-165) becomes a per-tile histogram whose
 // cross-tile prefix is found by decoupled look-back instead of a serial
 // Q x 256 prefix, and its de-randomised per-bin write buffers
-// (PermuteDerandomizedNew, :169-212) become a tile staged by bin in shared
+// (PermuteDerandomizedNew, :169-212) become a tile sorted by digit in shared
 // memory and written out in bin-contiguous runs.
 //
 // Per CTA (one tile of TILE = BLOCK * ITEMS keys):
-//   1. take the next tile ticket (tiles are handed out in launch order, so
-//      every tile a CTA waits on in step 4 is owned by a CTA already running);
+//   1. take the next tile ticket (tickets are handed out in launch order, so
+//      every tile a CTA waits on in step 5 is owned by a CTA already running);
 //   2. bulk-copy the tile global -> shared with the TMA engine, completing on
-//      an mbarrier (plain loads for the <16-byte ragged end, or when a
-//      buffer is not 16-byte aligned);
-//   3. rank: each warp owns a contiguous 32 * ITEMS run of the tile; for each
-//      item, __match_any_sync groups lanes holding the same digit, the group
-//      leader bumps the warp's shared counter for that digit, and lanes take
-//      rank = counter + peers below them.  Items are visited in tile order, so
-//      ranks preserve input order (stability);
-//   4. per bin: prefix of the warp counters, publish the tile's count
-//      (AGGREGATE), walk back over earlier tiles' words until an INCLUSIVE
-//      one, publish INCLUSIVE;
-//   5. write keys into shared memory at their in-tile sorted position;
+//      an mbarrier (plain loads for the <16-byte ragged end, or when a buffer
+//      is not 16-byte aligned); a partial tile is padded with all-ones keys,
+//      which sort after every real key;
+//   3. sort the tile by the 8-bit digit in shared memory as two stable 4-bit
+//      counting passes (low nibble, then high nibble).  Each thread owns ITEMS
+//      consecutive keys, so (thread, item) order is input order; per-thread
+//      counters live in shared memory at [nibble][thread], one bank per
+//      thread, so counting is conflict-free and needs no warp-wide matching;
+//      a block-wide exclusive scan of the counters gives each key its
+//      position;
+//   4. bin counts of the tile from the run boundaries of the sorted tile;
+//      publish them (AGGREGATE, or INCLUSIVE for tile 0);
+//   5. per bin, walk back over earlier tiles' words, four tiles per round
+//      trip, until an INCLUSIVE one; publish INCLUSIVE;
 //   6. write the sorted tile out: consecutive threads write consecutive keys
 //      of a bin to consecutive addresses.
 #include <cstdio>
+#include <cstdlib>
 
 #include "pa_common.cuh"
 #include "pa_kernels.cuh"
@@ -36,6 +40,8 @@ namespace {
 
 constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
+constexpr int kNibbleBins = 16;
+constexpr int kLookbackWidth = 4;  // predecessor tiles read per round trip
 
 template <typename S>
 struct StatusWord;
@@ -60,25 +66,154 @@ struct Geometry {
   static constexpr int kTile = BLOCK * ITEMS;
   static constexpr size_t kKeysOff = 0;
   static constexpr size_t kValsOff = kKeysOff + (size_t)kTile * sizeof(K);
-  static constexpr size_t kWarpHistOff = kValsOff + (HAS_VALS ? (size_t)kTile * 4 : 0);
-  static constexpr size_t kBinBaseOff = kWarpHistOff + (size_t)kWarps * kRadix * 4;
-  static constexpr size_t kTileCountOff = kBinBaseOff + (size_t)kRadix * 8;
-  static constexpr size_t kTileStartOff = kTileCountOff + (size_t)kRadix * 4;
-  static constexpr size_t kExclOff = kTileStartOff + (size_t)kRadix * 4;
-  static constexpr size_t kBarOff = kExclOff + (size_t)kRadix * 8;
+  static constexpr size_t kCntOff = kValsOff + (HAS_VALS ? (size_t)kTile * 4 : 0);
+  // counter (nibble s, thread t) lives at word s * kCntRow + t + t / 32
+  static constexpr int kCntRow = BLOCK + 32;
+  static constexpr size_t kBinBaseOff = kCntOff + (size_t)kNibbleBins * kCntRow * 4;
+  static constexpr size_t kBinStartOff = kBinBaseOff + (size_t)kRadix * 8;
+  static constexpr size_t kBinEndOff = kBinStartOff + (size_t)kRadix * 4;
+  static constexpr size_t kWarpTotOff = kBinEndOff + (size_t)kRadix * 4;
+  static constexpr size_t kBarOff = kWarpTotOff + (size_t)kWarps * 4 + 8 - ((size_t)kWarps * 4) % 8;
   static constexpr size_t kTileIdOff = kBarOff + 8;
   static constexpr size_t kAbortOff = kTileIdOff + 4;
   static constexpr size_t kBytes = kAbortOff + 4;
-  static_assert(kTile % 4 == 0, "tile must keep 16-byte alignment of tile starts");
+  static_assert(kTile % 4 == 0, "tile starts must stay 16-byte aligned");
+  static_assert((ITEMS * sizeof(K)) % 16 == 0, "a thread's run of keys is read as 16-byte vectors");
   static_assert(BLOCK >= kRadix, "one thread per bin in the look-back");
+  static_assert(ITEMS <= 16, "per-thread ranks are packed in 4 bits");
 };
 
-template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, typename S>
-__global__ void __launch_bounds__(BLOCK) onesweep_kernel(const OnesweepArgs args) {
+// Block-wide exclusive scan of one value per thread; also returns the total.
+// Contains one __syncthreads(); s_warp holds BLOCK / 32 words.
+template <int BLOCK>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t& total) {
+  constexpr int W = BLOCK / 32;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= (uint32_t)o) incl += t;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  uint32_t base = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    const uint32_t x = s_warp[w];
+    base += (uint32_t)w < warp ? x : 0u;
+    tot += x;
+  }
+  total = tot;
+  return base + incl - v;
+}
+
+// Counter word of (nibble s, thread t).  Rows are a multiple of 32 words and
+// each warp's 32 columns are shifted by one bank per warp, so that both
+// access patterns are free of bank conflicts: counting (a warp touches 32
+// different threads' columns, any nibbles) and the scan (a warp walks one
+// row, each lane 16 consecutive words).
+template <int BLOCK>
+__device__ __forceinline__ uint32_t cnt_index(uint32_t s, uint32_t t) {
+  return s * (uint32_t)(BLOCK + 32) + t + (t >> 5);
+}
+
+// One stable counting pass over the tile on the 4-bit nibble at `sh`: keys
+// (and payloads) held by each thread in `k` / `v` are written to their
+// nibble-sorted positions in s_keys / s_vals.  Ends with a barrier, after
+// which the tile in shared memory is in the new order.
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS>
+__device__ __forceinline__ void nibble_pass(const K (&k)[ITEMS], const uint32_t (&v)[HAS_VALS ? ITEMS : 1],
+                                            uint32_t sh, K* s_keys, uint32_t* s_vals, uint32_t* s_cnt,
+                                            uint32_t* s_warp) {
+  const uint32_t tid = threadIdx.x;
+  // This thread's column of counters; only this thread touches it until
+  // the scan.
+#pragma unroll
+  for (int s = 0; s < kNibbleBins; ++s) s_cnt[cnt_index<BLOCK>(s, tid)] = 0;
+  // Rank of each key among this thread's earlier keys of the same nibble
+  // (at most ITEMS - 1 <= 15), packed four bits per key.
+  uint32_t r[(ITEMS + 7) / 8];
+#pragma unroll
+  for (int q = 0; q < (ITEMS + 7) / 8; ++q) r[q] = 0;
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    uint32_t* c = s_cnt + cnt_index<BLOCK>((uint32_t)(k[j] >> sh) & 15u, tid);
+    const uint32_t x = *c;
+    r[j / 8] |= x << (4 * (j % 8));
+    *c = x + 1;
+  }
+  __syncthreads();
+  // Exclusive scan of the 16 x BLOCK counters in (nibble, thread) order:
+  // thread t owns the 16 consecutive counters [16t, 16t + 16) of that order.
+  const uint32_t lin = 16u * tid;
+  const uint32_t row = lin / BLOCK, col0 = lin % BLOCK;
+  uint32_t* cbase = s_cnt + row * (uint32_t)(BLOCK + 32);
+  uint32_t c[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const uint32_t col = col0 + i;
+    c[i] = cbase[col + (col >> 5)];
+  }
+  uint32_t run = 0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const uint32_t t = c[i];
+    c[i] = run;
+    run += t;
+  }
+  uint32_t total;
+  const uint32_t base = block_exclusive_scan<BLOCK>(run, s_warp, total);
+  (void)total;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const uint32_t col = col0 + i;
+    cbase[col + (col >> 5)] = c[i] + base;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    const uint32_t pos =
+        s_cnt[cnt_index<BLOCK>((uint32_t)(k[j] >> sh) & 15u, tid)] + ((r[j / 8] >> (4 * (j % 8))) & 15u);
+    s_keys[pos] = k[j];
+    if (HAS_VALS) s_vals[pos] = v[j];
+  }
+  __syncthreads();
+}
+
+// Loads this thread's ITEMS consecutive keys (and payloads) from shared
+// memory with 16-byte vector reads.
+template <typename K, bool HAS_VALS, int ITEMS>
+__device__ __forceinline__ void load_run(K (&k)[ITEMS], uint32_t (&v)[HAS_VALS ? ITEMS : 1], const K* s_keys,
+                                         const uint32_t* s_vals) {
+  const uint4* src = reinterpret_cast<const uint4*>(s_keys + threadIdx.x * ITEMS);
+  constexpr int PER = 16 / (int)sizeof(K);
+#pragma unroll
+  for (int q = 0; q < ITEMS / PER; ++q) {
+    const uint4 x = src[q];
+    const K* e = reinterpret_cast<const K*>(&x);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) k[q * PER + i] = e[i];
+  }
+  if (HAS_VALS) {
+    const uint4* vs = reinterpret_cast<const uint4*>(s_vals + threadIdx.x * ITEMS);
+#pragma unroll
+    for (int q = 0; q < ITEMS / 4; ++q) {
+      const uint4 x = vs[q];
+      v[4 * q + 0] = x.x;
+      v[4 * q + 1] = x.y;
+      v[4 * q + 2] = x.z;
+      v[4 * q + 3] = x.w;
+    }
+  }
+}
+
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S>
+__global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArgs args) {
   using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
   using SW = StatusWord<S>;
   constexpr int TILE = G::kTile;
-  constexpr uint32_t FULL = 0xFFFFFFFFu;
+  constexpr uint32_t kDigitMask = kRadix - 1;
 
   const PassCtrl pc = args.ctrl->pass[args.pass];
   if (pc.skip) return;
@@ -86,11 +221,11 @@ __global__ void __launch_bounds__(BLOCK) onesweep_kernel(const OnesweepArgs args
   extern __shared__ __align__(128) unsigned char smem[];
   K* s_keys = reinterpret_cast<K*>(smem + G::kKeysOff);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + G::kValsOff);
-  uint32_t* s_wh = reinterpret_cast<uint32_t*>(smem + G::kWarpHistOff);
+  uint32_t* s_cnt = reinterpret_cast<uint32_t*>(smem + G::kCntOff);
   unsigned long long* s_bin_base = reinterpret_cast<unsigned long long*>(smem + G::kBinBaseOff);
-  uint32_t* s_tile_count = reinterpret_cast<uint32_t*>(smem + G::kTileCountOff);
-  uint32_t* s_tile_start = reinterpret_cast<uint32_t*>(smem + G::kTileStartOff);
-  unsigned long long* s_excl = reinterpret_cast<unsigned long long*>(smem + G::kExclOff);
+  uint32_t* s_bin_start = reinterpret_cast<uint32_t*>(smem + G::kBinStartOff);
+  uint32_t* s_bin_end = reinterpret_cast<uint32_t*>(smem + G::kBinEndOff);
+  uint32_t* s_warp = reinterpret_cast<uint32_t*>(smem + G::kWarpTotOff);
   uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + G::kBarOff);
   uint32_t* s_tile_id = reinterpret_cast<uint32_t*>(smem + G::kTileIdOff);
   uint32_t* s_abort = reinterpret_cast<uint32_t*>(smem + G::kAbortOff);
@@ -102,20 +237,16 @@ __global__ void __launch_bounds__(BLOCK) onesweep_kernel(const OnesweepArgs args
   const bool tin = args.is_float && pc.transform_in;
   const bool tout = args.is_float && pc.transform_out;
   const uint32_t shift = args.shift;
-
   const uint32_t tid = threadIdx.x;
-  const uint32_t warp = tid >> 5;
-  const uint32_t lane = tid & 31u;
 
+  // ---- 1. ticket -------------------------------------------------------------
   if (tid == 0) {
     *s_tile_id = atomicAdd(args.tile_counter, 1u);
     *s_abort = 0;
     mbar_init(s_bar, 1);
     mbar_fence_init();
   }
-  for (uint32_t i = tid; i < (uint32_t)(G::kWarps * kRadix); i += BLOCK) s_wh[i] = 0;
   __syncthreads();
-
   const uint32_t tile = *s_tile_id;
   const size_t num_tiles = (args.n + TILE - 1) / TILE;
   if ((size_t)tile >= num_tiles) {  // a ticket counter that was not reset
@@ -125,9 +256,10 @@ __global__ void __launch_bounds__(BLOCK) onesweep_kernel(const OnesweepArgs args
   const size_t tile_base = (size_t)tile * TILE;
   const uint32_t tile_n = (uint32_t)min((size_t)TILE, args.n - tile_base);
 
-  // ---- 2. load the tile into shared memory ---------------------------------
+  // ---- 2. tile -> shared memory ---------------------------------------------
   const bool tma_ok = ((reinterpret_cast<uintptr_t>(in) & 15u) == 0) &&
                       (!HAS_VALS || (reinterpret_cast<uintptr_t>(vin) & 15u) == 0);
+  uint32_t loaded = 0;  // keys [0, loaded) arrive by bulk copy
   if (tma_ok) {
     const uint32_t kbulk = (tile_n * (uint32_t)sizeof(K)) & ~15u;
     const uint32_t vbulk = HAS_VALS ? ((tile_n * 4u) & ~15u) : 0u;
@@ -136,140 +268,113 @@ __global__ void __launch_bounds__(BLOCK) onesweep_kernel(const OnesweepArgs args
       if (kbulk) bulk_load_g2s(s_keys, in + tile_base, kbulk, s_bar);
       if (HAS_VALS && vbulk) bulk_load_g2s(s_vals, vin + tile_base, vbulk, s_bar);
     }
-    for (uint32_t i = kbulk / (uint32_t)sizeof(K) + tid; i < tile_n; i += BLOCK) s_keys[i] = in[tile_base + i];
+    loaded = kbulk / (uint32_t)sizeof(K);
     if (HAS_VALS)
       for (uint32_t i = vbulk / 4u + tid; i < tile_n; i += BLOCK) s_vals[i] = vin[tile_base + i];
-    mbar_wait_bounded(s_bar, 0, args.err);
-  } else {
-    for (uint32_t i = tid; i < tile_n; i += BLOCK) s_keys[i] = in[tile_base + i];
-    if (HAS_VALS)
-      for (uint32_t i = tid; i < tile_n; i += BLOCK) s_vals[i] = vin[tile_base + i];
+  } else if (HAS_VALS) {
+    for (uint32_t i = tid; i < tile_n; i += BLOCK) s_vals[i] = vin[tile_base + i];
   }
+  for (uint32_t i = loaded + tid; i < tile_n; i += BLOCK) s_keys[i] = in[tile_base + i];
+  // padding: all-ones keys sort after every real key of any digit
+  for (uint32_t i = tile_n + tid; i < (uint32_t)TILE; i += BLOCK) s_keys[i] = ~(K)0;
+  for (uint32_t i = tid; i < (uint32_t)kRadix; i += BLOCK) {
+    s_bin_start[i] = 0;
+    s_bin_end[i] = 0;
+  }
+  if (tma_ok && !mbar_wait_bounded(s_bar, 0, args.err)) *s_abort = 1;
   __syncthreads();
 
-  // ---- 3. rank within the warp -------------------------------------------
-  const bool full = tile_n == (uint32_t)TILE;
-  const uint32_t wbase = warp * ITEMS * 32;
+  // ---- 3. sort the tile by the digit: low nibble, then high nibble ------------
   K k[ITEMS];
   uint32_t v[HAS_VALS ? ITEMS : 1];
-  uint32_t rank[ITEMS];
-  uint32_t* wh = s_wh + warp * kRadix;
-  const uint32_t lt = lanemask_lt();
+  load_run<K, HAS_VALS, ITEMS>(k, v, s_keys, s_vals);
+  if (tin) {
+    const uint32_t first = tid * ITEMS;
 #pragma unroll
-  for (int j = 0; j < ITEMS; ++j) {
-    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
-    const bool valid = full || idx < tile_n;
-    k[j] = valid ? to_ordered(s_keys[idx], tin) : (K)0;
-    if (HAS_VALS) v[j] = valid ? s_vals[idx] : 0u;
+    for (int j = 0; j < ITEMS; ++j)
+      if (first + j < tile_n) k[j] = to_ordered(k[j], true);
   }
-#pragma unroll
-  for (int j = 0; j < ITEMS; ++j) {
-    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
-    const bool valid = full || idx < tile_n;
-    const uint32_t d = valid ? digit_of(k[j], shift, kRadix - 1) : (uint32_t)kRadix;
-    const uint32_t peers = __match_any_sync(FULL, d);
-    const uint32_t leader = __ffs(peers) - 1;
-    uint32_t base = 0;
-    if (lane == leader && valid) {
-      base = wh[d];
-      wh[d] = base + __popc(peers);
-    }
-    base = __shfl_sync(FULL, base, leader);
-    rank[j] = base + __popc(peers & lt);
-    __syncwarp();
-  }
-  __syncthreads();
+  nibble_pass<K, HAS_VALS, BLOCK, ITEMS>(k, v, shift, s_keys, s_vals, s_cnt, s_warp);
+  load_run<K, HAS_VALS, ITEMS>(k, v, s_keys, s_vals);
+  nibble_pass<K, HAS_VALS, BLOCK, ITEMS>(k, v, shift + 4, s_keys, s_vals, s_cnt, s_warp);
 
-  // ---- 4. tile counts, publish, look-back --------------------------------
-  if (tid < kRadix) {
-    uint32_t sum = 0;
-#pragma unroll 4
-    for (int w = 0; w < G::kWarps; ++w) {
-      const uint32_t c = s_wh[w * kRadix + tid];
-      s_wh[w * kRadix + tid] = sum;
-      sum += c;
+  // ---- 4. bin counts from run boundaries; publish --------------------------
+  {
+    const uint32_t first = tid * ITEMS;
+    K run[ITEMS];
+    uint32_t unused[1];
+    load_run<K, false, ITEMS>(run, unused, s_keys, nullptr);
+    uint32_t prev = first > 0 ? digit_of(s_keys[first - 1], shift, kDigitMask) : 0xFFFFFFFFu;
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+      const uint32_t i = first + j;
+      if (i < tile_n) {
+        const uint32_t d = digit_of(run[j], shift, kDigitMask);
+        if (d != prev) {
+          s_bin_start[d] = i;
+          if (i > 0) s_bin_end[prev] = i;
+        }
+        if (i + 1 == tile_n) s_bin_end[d] = tile_n;
+        prev = d;
+      }
     }
-    s_tile_count[tid] = sum;
-    S* st = static_cast<S*>(args.status) + (size_t)tile * kRadix + tid;
-    st_relaxed_gpu(st, (S)((tile == 0 ? SW::kIncl : SW::kAgg) | (S)sum));
   }
   __syncthreads();
-  if (warp == 0) {
-    // exclusive scan of the 256 tile counts: 8 consecutive bins per lane
-    uint32_t c[kRadix / 32];
-    uint32_t local = 0;
-#pragma unroll
-    for (int i = 0; i < kRadix / 32; ++i) {
-      c[i] = s_tile_count[lane * (kRadix / 32) + i];
-      local += c[i];
-    }
-    uint32_t incl = local;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(FULL, incl, o);
-      if (lane >= (uint32_t)o) incl += t;
-    }
-    uint32_t run = incl - local;
-#pragma unroll
-    for (int i = 0; i < kRadix / 32; ++i) {
-      s_tile_start[lane * (kRadix / 32) + i] = run;
-      run += c[i];
-    }
+  uint32_t count = 0;
+  if (tid < (uint32_t)kRadix) {
+    count = s_bin_end[tid] - s_bin_start[tid];
+    S* st = static_cast<S*>(args.status) + (size_t)tile * kRadix + tid;
+    st_relaxed_gpu(st, (S)((tile == 0 ? SW::kIncl : SW::kAgg) | (S)count));
   }
-  if (tid < kRadix) {
+
+  // ---- 5. decoupled look-back ---------------------------------------------
+  if (tid < (uint32_t)kRadix) {
     unsigned long long excl = 0;
     if (tile > 0) {
       const S* base = static_cast<const S*>(args.status) + tid;
       long long t = (long long)tile - 1;
       uint32_t spins = 0;
-      while (true) {
-        const S s = ld_relaxed_gpu(base + (size_t)t * kRadix);
-        const uint32_t flag = (uint32_t)(s >> SW::kShift);
-        if (flag == 0) {
-          if (++spins > kSpinLimit) {
-            raise_error(args.err, DEVERR_LOOKBACK_TIMEOUT);
-            *s_abort = 1;
-            break;
-          }
-          continue;
+      bool done = false;
+      while (!done) {
+        S s[kLookbackWidth];
+#pragma unroll
+        for (int i = 0; i < kLookbackWidth; ++i)
+          s[i] = (t - i >= 0) ? ld_relaxed_gpu(base + (size_t)(t - i) * kRadix) : (S)SW::kIncl;
+        int used = 0;
+#pragma unroll
+        for (int i = 0; i < kLookbackWidth; ++i) {
+          if (done || used != i) break;
+          const uint32_t flag = (uint32_t)(s[i] >> SW::kShift);
+          if (flag == 0) break;
+          excl += (unsigned long long)(s[i] & SW::kMask);
+          ++used;
+          if (flag == 2u) done = true;
         }
-        excl += (unsigned long long)(s & SW::kMask);
-        if (flag == 2u || t == 0) break;
-        --t;
+        t -= used;
+        if (!done && used == 0 && ++spins > kSpinLimit) {
+          raise_error(args.err, DEVERR_LOOKBACK_TIMEOUT);
+          *s_abort = 1;
+          break;
+        }
       }
       S* st = static_cast<S*>(args.status) + (size_t)tile * kRadix + tid;
-      st_relaxed_gpu(st, (S)(SW::kIncl | (S)(excl + s_tile_count[tid])));
+      st_relaxed_gpu(st, (S)(SW::kIncl | (S)(excl + count)));
     }
-    s_excl[tid] = excl;
+    s_bin_base[tid] = args.bin_start[tid] + excl - (unsigned long long)s_bin_start[tid];
   }
   __syncthreads();
 
-  // ---- 5. stage by bin in shared memory ----------------------------------
-  if (tid < kRadix) s_bin_base[tid] = args.bin_start[tid] + s_excl[tid] - (unsigned long long)s_tile_start[tid];
-#pragma unroll
-  for (int j = 0; j < ITEMS; ++j) {
-    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
-    if (full || idx < tile_n) {
-      const uint32_t d = digit_of(k[j], shift, kRadix - 1);
-      const uint32_t pos = s_tile_start[d] + wh[d] + rank[j];
-      s_keys[pos] = k[j];
-      if (HAS_VALS) s_vals[pos] = v[j];
-    }
-  }
-  __syncthreads();
-
-  // ---- 6. write out in bin-contiguous runs --------------------------------
-  // A tile whose look-back gave up has no valid offsets: it writes nothing
-  // (the call reports the failure), and every store is bounds-checked.
+  // ---- 6. write out in bin-contiguous runs -----------------------------------
+  // A tile whose look-back or load gave up has no valid offsets: it writes
+  // nothing (the call reports the failure), and every store is bounds-checked.
   if (*s_abort) return;
   const unsigned long long n_out = args.n;
-#pragma unroll
+#pragma unroll 4
   for (int j = 0; j < ITEMS; ++j) {
     const uint32_t i = (uint32_t)j * BLOCK + tid;
-    if (full || i < tile_n) {
+    if (i < tile_n) {
       const K key = s_keys[i];
-      const uint32_t d = digit_of(key, shift, kRadix - 1);
-      const unsigned long long o = s_bin_base[d] + i;
+      const unsigned long long o = s_bin_base[digit_of(key, shift, kDigitMask)] + i;
       if (o < n_out) {
         out[o] = from_ordered(key, tout);
         if (HAS_VALS) vout[o] = s_vals[i];
@@ -289,19 +394,38 @@ __global__ void final_copy_kernel(K* keys_a, const K* keys_b, uint32_t* vals_a, 
   }
 }
 
-// Tile geometry per key type.  32-bit keys: 512 threads x 16 keys; wider
-// records use fewer items per thread so that keys, payloads and ranks stay
-// in registers.
-constexpr int kBlock = 512;
-constexpr int kItemsU32 = 16;
-constexpr int kItemsU32Kv = 12;
-constexpr int kItemsU64 = 12;
-constexpr int kItemsU64Kv = 8;
+// Tile geometries.  Each is (threads, keys per thread, CTAs per SM the
+// register budget is cut for).  The active one per (key type, payload) is
+// the first entry unless PA_ONESWEEP_GEOMETRY selects another (tuning).
+struct GeomChoice {
+  int block, items, minb;
+};
+constexpr GeomChoice kGeomU32[] = {{512, 16, 2}, {256, 16, 4}, {384, 16, 3}, {1024, 8, 1}, {512, 8, 3}};
+constexpr GeomChoice kGeomU32Kv[] = {{256, 12, 4}, {512, 12, 2}, {512, 8, 3}};
+constexpr GeomChoice kGeomU64[] = {{256, 12, 4}, {512, 12, 2}, {512, 8, 3}};
+constexpr GeomChoice kGeomU64Kv[] = {{256, 12, 3}, {256, 8, 4}, {512, 8, 2}};
 
-template <typename K, bool HAS_VALS, int ITEMS, typename S>
-cudaError_t launch_t(const OnesweepArgs& a, cudaStream_t stream) {
-  using G = Geometry<K, HAS_VALS, kBlock, ITEMS>;
-  auto kern = onesweep_kernel<K, HAS_VALS, kBlock, ITEMS, S>;
+int geometry_index(int count) {
+  static int idx = -2;
+  if (idx == -2) {
+    const char* e = std::getenv("PA_ONESWEEP_GEOMETRY");
+    idx = e ? std::atoi(e) : 0;
+  }
+  return (idx >= 0 && idx < count) ? idx : 0;
+}
+
+template <typename K, bool HAS_VALS>
+GeomChoice active_geometry() {
+  if (sizeof(K) == 4 && !HAS_VALS) return kGeomU32[geometry_index(5)];
+  if (sizeof(K) == 4) return kGeomU32Kv[geometry_index(3)];
+  if (!HAS_VALS) return kGeomU64[geometry_index(3)];
+  return kGeomU64Kv[geometry_index(3)];
+}
+
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S>
+cudaError_t launch_g(const OnesweepArgs& a, cudaStream_t stream) {
+  using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
+  auto kern = onesweep_kernel<K, HAS_VALS, BLOCK, ITEMS, MINB, S>;
   static bool configured = false;  // one attribute call per instantiation
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kBytes);
@@ -309,33 +433,61 @@ cudaError_t launch_t(const OnesweepArgs& a, cudaStream_t stream) {
     configured = true;
   }
   const size_t tiles = ceil_div(a.n, (size_t)G::kTile);
-  kern<<<(unsigned)tiles, kBlock, G::kBytes, stream>>>(a);
+  kern<<<(unsigned)tiles, BLOCK, G::kBytes, stream>>>(a);
   return cudaGetLastError();
 }
 
-template <typename K, bool HAS_VALS, int ITEMS>
-cudaError_t launch_k(const OnesweepArgs& a, cudaStream_t stream) {
-  if (a.n < (1ull << 30)) return launch_t<K, HAS_VALS, ITEMS, uint32_t>(a, stream);
-  return launch_t<K, HAS_VALS, ITEMS, unsigned long long>(a, stream);
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB>
+cudaError_t launch_s(const OnesweepArgs& a, cudaStream_t stream) {
+  if (a.n < (1ull << 30)) return launch_g<K, HAS_VALS, BLOCK, ITEMS, MINB, uint32_t>(a, stream);
+  return launch_g<K, HAS_VALS, BLOCK, ITEMS, MINB, unsigned long long>(a, stream);
+}
+
+#define PA_GEOM_CASE(B, I, M) \
+  if (g.block == B && g.items == I && g.minb == M) return launch_s<K, HAS_VALS, B, I, M>(a, stream);
+
+template <typename K, bool HAS_VALS>
+cudaError_t launch_kv(const OnesweepArgs& a, cudaStream_t stream) {
+  const GeomChoice g = active_geometry<K, HAS_VALS>();
+  if constexpr (sizeof(K) == 4 && !HAS_VALS) {
+    PA_GEOM_CASE(512, 16, 2)
+    PA_GEOM_CASE(256, 16, 4)
+    PA_GEOM_CASE(384, 16, 3)
+    PA_GEOM_CASE(1024, 8, 1)
+    PA_GEOM_CASE(512, 8, 3)
+  } else if constexpr (sizeof(K) == 4) {
+    PA_GEOM_CASE(256, 12, 4)
+    PA_GEOM_CASE(512, 12, 2)
+    PA_GEOM_CASE(512, 8, 3)
+  } else if constexpr (!HAS_VALS) {
+    PA_GEOM_CASE(256, 12, 4)
+    PA_GEOM_CASE(512, 12, 2)
+    PA_GEOM_CASE(512, 8, 3)
+  } else {
+    PA_GEOM_CASE(256, 12, 3)
+    PA_GEOM_CASE(256, 8, 4)
+    PA_GEOM_CASE(512, 8, 2)
+  }
+  return cudaErrorInvalidConfiguration;
 }
 
 }  // namespace
 
 size_t onesweep_tile_keys(int key_bytes, bool has_vals) {
-  if (key_bytes == 4) return (size_t)kBlock * (has_vals ? kItemsU32Kv : kItemsU32);
-  return (size_t)kBlock * (has_vals ? kItemsU64Kv : kItemsU64);
+  GeomChoice g;
+  if (key_bytes == 4)
+    g = has_vals ? active_geometry<uint32_t, true>() : active_geometry<uint32_t, false>();
+  else
+    g = has_vals ? active_geometry<unsigned long long, true>() : active_geometry<unsigned long long, false>();
+  return (size_t)g.block * g.items;
 }
 
 size_t onesweep_status_bytes(size_t n) { return n < (1ull << 30) ? 4 : 8; }
 
 cudaError_t launch_onesweep_pass(const OnesweepArgs& a, int key_bytes, bool has_vals, cudaStream_t stream) {
   if (a.n == 0) return cudaSuccess;
-  if (key_bytes == 4) {
-    return has_vals ? launch_k<uint32_t, true, kItemsU32Kv>(a, stream)
-                    : launch_k<uint32_t, false, kItemsU32>(a, stream);
-  }
-  return has_vals ? launch_k<unsigned long long, true, kItemsU64Kv>(a, stream)
-                  : launch_k<unsigned long long, false, kItemsU64>(a, stream);
+  if (key_bytes == 4) return has_vals ? launch_kv<uint32_t, true>(a, stream) : launch_kv<uint32_t, false>(a, stream);
+  return has_vals ? launch_kv<unsigned long long, true>(a, stream) : launch_kv<unsigned long long, false>(a, stream);
 }
 
 cudaError_t launch_final_copy(void* keys_a, const void* keys_b, uint32_t* vals_a, const uint32_t* vals_b,
