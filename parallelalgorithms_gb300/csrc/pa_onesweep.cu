@@ -83,40 +83,51 @@ struct Geometry {
   static_assert(ITEMS <= 16, "per-thread ranks are packed in 4 bits");
 };
 
-// Block-wide exclusive scan of one value per thread; also returns the total.
-// Contains one __syncthreads(); s_warp holds BLOCK / 32 words.
+// Block-wide exclusive scan of one value per thread.  Contains one
+// __syncthreads(); s_warp holds BLOCK / 32 words.
 template <int BLOCK>
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t& total) {
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp) {
   constexpr int W = BLOCK / 32;
+  constexpr uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   uint32_t incl = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    const uint32_t t = __shfl_up_sync(FULL, incl, o);
     if (lane >= (uint32_t)o) incl += t;
   }
   if (lane == 31) s_warp[warp] = incl;
   __syncthreads();
-  uint32_t base = 0, tot = 0;
+  // every warp scans the W warp totals, lane l holding total l
+  const uint32_t wt = lane < (uint32_t)W ? s_warp[lane] : 0u;
+  uint32_t wincl = wt;
 #pragma unroll
-  for (int w = 0; w < W; ++w) {
-    const uint32_t x = s_warp[w];
-    base += (uint32_t)w < warp ? x : 0u;
-    tot += x;
+  for (int o = 1; o < W; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(FULL, wincl, o);
+    if (lane >= (uint32_t)o) wincl += t;
   }
-  total = tot;
-  return base + incl - v;
+  return __shfl_sync(FULL, wincl - wt, warp) + incl - v;
 }
 
-// Counter word of (nibble s, thread t).  Rows are a multiple of 32 words and
-// each warp's 32 columns are shifted by one bank per warp, so that both
-// access patterns are free of bank conflicts: counting (a warp touches 32
-// different threads' columns, any nibbles) and the scan (a warp walks one
-// row, each lane 16 consecutive words).
-template <int BLOCK>
-__device__ __forceinline__ uint32_t cnt_index(uint32_t s, uint32_t t) {
-  return s * (uint32_t)(BLOCK + 32) + t + (t >> 5);
+// Byte `shift / 8` of a key (digits are byte aligned): one byte-permute.
+template <typename K>
+__device__ __forceinline__ uint32_t digit8(K key, uint32_t sel, bool upper) {
+  uint32_t w;
+  if constexpr (sizeof(K) == 4) {
+    (void)upper;
+    w = (uint32_t)key;
+  } else {
+    w = upper ? (uint32_t)(key >> 32) : (uint32_t)key;
+  }
+  return __byte_perm(w, 0u, sel);
 }
+
+// Counters: (nibble s, thread t) lives at word s * (BLOCK + 32) + t + t / 32.
+// Rows are a multiple of 32 words and each warp's 32 columns are shifted by
+// one bank per warp, so that both access patterns are free of bank
+// conflicts: counting (a warp touches 32 different threads' columns, any
+// nibbles) and the scan (a warp walks one row, each lane 16 consecutive
+// words).
 
 // One stable counting pass over the tile on the 4-bit nibble at `sh`: keys
 // (and payloads) held by each thread in `k` / `v` are written to their
@@ -127,10 +138,10 @@ __device__ __forceinline__ void nibble_pass(const K (&k)[ITEMS], const uint32_t 
                                             uint32_t sh, K* s_keys, uint32_t* s_vals, uint32_t* s_cnt,
                                             uint32_t* s_warp) {
   const uint32_t tid = threadIdx.x;
-  // This thread's column of counters; only this thread touches it until
-  // the scan.
+  uint32_t* col = s_cnt + tid + (tid >> 5);  // this thread's column: word col[s * (BLOCK + 32)]
+  // Only this thread touches its column until the scan.
 #pragma unroll
-  for (int s = 0; s < kNibbleBins; ++s) s_cnt[cnt_index<BLOCK>(s, tid)] = 0;
+  for (int s = 0; s < kNibbleBins; ++s) col[s * (BLOCK + 32)] = 0;
   // Rank of each key among this thread's earlier keys of the same nibble
   // (at most ITEMS - 1 <= 15), packed four bits per key.
   uint32_t r[(ITEMS + 7) / 8];
@@ -138,23 +149,22 @@ __device__ __forceinline__ void nibble_pass(const K (&k)[ITEMS], const uint32_t 
   for (int q = 0; q < (ITEMS + 7) / 8; ++q) r[q] = 0;
 #pragma unroll
   for (int j = 0; j < ITEMS; ++j) {
-    uint32_t* c = s_cnt + cnt_index<BLOCK>((uint32_t)(k[j] >> sh) & 15u, tid);
+    uint32_t* c = col + ((uint32_t)(k[j] >> sh) & 15u) * (uint32_t)(BLOCK + 32);
     const uint32_t x = *c;
-    r[j / 8] |= x << (4 * (j % 8));
+    r[j / 8] += x << (4 * (j % 8));
     *c = x + 1;
   }
   __syncthreads();
   // Exclusive scan of the 16 x BLOCK counters in (nibble, thread) order:
-  // thread t owns the 16 consecutive counters [16t, 16t + 16) of that order.
+  // thread t owns the 16 consecutive counters [16t, 16t + 16) of that order,
+  // which sit in one row at consecutive words (a 16-aligned run of columns
+  // never crosses a 32-column group).
   const uint32_t lin = 16u * tid;
   const uint32_t row = lin / BLOCK, col0 = lin % BLOCK;
-  uint32_t* cbase = s_cnt + row * (uint32_t)(BLOCK + 32);
+  uint32_t* cb = s_cnt + row * (uint32_t)(BLOCK + 32) + col0 + (col0 >> 5);
   uint32_t c[16];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const uint32_t col = col0 + i;
-    c[i] = cbase[col + (col >> 5)];
-  }
+  for (int i = 0; i < 16; ++i) c[i] = cb[i];
   uint32_t run = 0;
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
@@ -162,19 +172,14 @@ __device__ __forceinline__ void nibble_pass(const K (&k)[ITEMS], const uint32_t 
     c[i] = run;
     run += t;
   }
-  uint32_t total;
-  const uint32_t base = block_exclusive_scan<BLOCK>(run, s_warp, total);
-  (void)total;
+  const uint32_t base = block_exclusive_scan<BLOCK>(run, s_warp);
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const uint32_t col = col0 + i;
-    cbase[col + (col >> 5)] = c[i] + base;
-  }
+  for (int i = 0; i < 16; ++i) cb[i] = c[i] + base;
   __syncthreads();
 #pragma unroll
   for (int j = 0; j < ITEMS; ++j) {
-    const uint32_t pos =
-        s_cnt[cnt_index<BLOCK>((uint32_t)(k[j] >> sh) & 15u, tid)] + ((r[j / 8] >> (4 * (j % 8))) & 15u);
+    const uint32_t pos = col[((uint32_t)(k[j] >> sh) & 15u) * (uint32_t)(BLOCK + 32)] +
+                         ((r[j / 8] >> (4 * (j % 8))) & 15u);
     s_keys[pos] = k[j];
     if (HAS_VALS) s_vals[pos] = v[j];
   }
@@ -213,7 +218,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
   using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
   using SW = StatusWord<S>;
   constexpr int TILE = G::kTile;
-  constexpr uint32_t kDigitMask = kRadix - 1;
 
   const PassCtrl pc = args.ctrl->pass[args.pass];
   if (pc.skip) return;
@@ -299,23 +303,39 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
   nibble_pass<K, HAS_VALS, BLOCK, ITEMS>(k, v, shift + 4, s_keys, s_vals, s_cnt, s_warp);
 
   // ---- 4. bin counts from run boundaries; publish --------------------------
+  const uint32_t dsel = 0x4440u | ((shift >> 3) & 3u);
+  const bool dupper = shift >= 32;
+  const bool full = tile_n == (uint32_t)TILE;
   {
     const uint32_t first = tid * ITEMS;
     K run[ITEMS];
     uint32_t unused[1];
     load_run<K, false, ITEMS>(run, unused, s_keys, nullptr);
-    uint32_t prev = first > 0 ? digit_of(s_keys[first - 1], shift, kDigitMask) : 0xFFFFFFFFu;
+    uint32_t prev = first > 0 ? digit8(s_keys[first - 1], dsel, dupper) : 0xFFFFFFFFu;
+    if (full) {
 #pragma unroll
-    for (int j = 0; j < ITEMS; ++j) {
-      const uint32_t i = first + j;
-      if (i < tile_n) {
-        const uint32_t d = digit_of(run[j], shift, kDigitMask);
+      for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t d = digit8(run[j], dsel, dupper);
         if (d != prev) {
-          s_bin_start[d] = i;
-          if (i > 0) s_bin_end[prev] = i;
+          s_bin_start[d] = first + j;
+          if (first + j > 0) s_bin_end[prev] = first + j;
         }
-        if (i + 1 == tile_n) s_bin_end[d] = tile_n;
         prev = d;
+      }
+      if (first + ITEMS == (uint32_t)TILE) s_bin_end[prev] = TILE;
+    } else {
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t i = first + j;
+        if (i < tile_n) {
+          const uint32_t d = digit8(run[j], dsel, dupper);
+          if (d != prev) {
+            s_bin_start[d] = i;
+            if (i > 0) s_bin_end[prev] = i;
+          }
+          if (i + 1 == tile_n) s_bin_end[d] = tile_n;
+          prev = d;
+        }
       }
     }
   }
@@ -328,25 +348,27 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
   }
 
   // ---- 5. decoupled look-back ---------------------------------------------
+  // Offsets are kept in the status word type: 32-bit when n < 2^30.
+  S* s_base = reinterpret_cast<S*>(s_bin_base);
   if (tid < (uint32_t)kRadix) {
-    unsigned long long excl = 0;
+    S excl = 0;
     if (tile > 0) {
       const S* base = static_cast<const S*>(args.status) + tid;
       long long t = (long long)tile - 1;
       uint32_t spins = 0;
       bool done = false;
       while (!done) {
-        S s[kLookbackWidth];
+        S sw[kLookbackWidth];
 #pragma unroll
         for (int i = 0; i < kLookbackWidth; ++i)
-          s[i] = (t - i >= 0) ? ld_relaxed_gpu(base + (size_t)(t - i) * kRadix) : (S)SW::kIncl;
+          sw[i] = (t - i >= 0) ? ld_relaxed_gpu(base + (size_t)(t - i) * kRadix) : (S)SW::kIncl;
         int used = 0;
 #pragma unroll
         for (int i = 0; i < kLookbackWidth; ++i) {
           if (done || used != i) break;
-          const uint32_t flag = (uint32_t)(s[i] >> SW::kShift);
+          const uint32_t flag = (uint32_t)(sw[i] >> SW::kShift);
           if (flag == 0) break;
-          excl += (unsigned long long)(s[i] & SW::kMask);
+          excl += sw[i] & SW::kMask;
           ++used;
           if (flag == 2u) done = true;
         }
@@ -360,7 +382,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
       S* st = static_cast<S*>(args.status) + (size_t)tile * kRadix + tid;
       st_relaxed_gpu(st, (S)(SW::kIncl | (S)(excl + count)));
     }
-    s_bin_base[tid] = args.bin_start[tid] + excl - (unsigned long long)s_bin_start[tid];
+    s_base[tid] = (S)args.bin_start[tid] + excl - (S)s_bin_start[tid];
   }
   __syncthreads();
 
@@ -368,19 +390,34 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
   // A tile whose look-back or load gave up has no valid offsets: it writes
   // nothing (the call reports the failure), and every store is bounds-checked.
   if (*s_abort) return;
-  const unsigned long long n_out = args.n;
+  const S n_out = (S)args.n;
+  auto scatter = [&](auto transform) {
+    if (full) {
 #pragma unroll 4
-  for (int j = 0; j < ITEMS; ++j) {
-    const uint32_t i = (uint32_t)j * BLOCK + tid;
-    if (i < tile_n) {
-      const K key = s_keys[i];
-      const unsigned long long o = s_bin_base[digit_of(key, shift, kDigitMask)] + i;
-      if (o < n_out) {
-        out[o] = from_ordered(key, tout);
-        if (HAS_VALS) vout[o] = s_vals[i];
+      for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t i = (uint32_t)j * BLOCK + tid;
+        const K key = s_keys[i];
+        const S o = s_base[digit8(key, dsel, dupper)] + i;
+        if (o < n_out) {
+          out[o] = transform(key);
+          if (HAS_VALS) vout[o] = s_vals[i];
+        }
+      }
+    } else {
+      for (uint32_t i = tid; i < tile_n; i += BLOCK) {
+        const K key = s_keys[i];
+        const S o = s_base[digit8(key, dsel, dupper)] + i;
+        if (o < n_out) {
+          out[o] = transform(key);
+          if (HAS_VALS) vout[o] = s_vals[i];
+        }
       }
     }
-  }
+  };
+  if (tout)
+    scatter([](K x) { return from_ordered(x, true); });
+  else
+    scatter([](K x) { return x; });
 }
 
 template <typename K>
@@ -401,7 +438,7 @@ struct GeomChoice {
   int block, items, minb;
 };
 constexpr GeomChoice kGeomU32[] = {{512, 16, 2}, {256, 16, 4}, {384, 16, 3}, {1024, 8, 1}, {512, 8, 3}};
-constexpr GeomChoice kGeomU32Kv[] = {{256, 12, 4}, {512, 12, 2}, {512, 8, 3}};
+constexpr GeomChoice kGeomU32Kv[] = {{512, 12, 2}, {256, 12, 4}, {512, 8, 3}};
 constexpr GeomChoice kGeomU64[] = {{256, 12, 4}, {512, 12, 2}, {512, 8, 3}};
 constexpr GeomChoice kGeomU64Kv[] = {{256, 12, 3}, {256, 8, 4}, {512, 8, 2}};
 
@@ -456,8 +493,8 @@ cudaError_t launch_kv(const OnesweepArgs& a, cudaStream_t stream) {
     PA_GEOM_CASE(1024, 8, 1)
     PA_GEOM_CASE(512, 8, 3)
   } else if constexpr (sizeof(K) == 4) {
-    PA_GEOM_CASE(256, 12, 4)
     PA_GEOM_CASE(512, 12, 2)
+    PA_GEOM_CASE(256, 12, 4)
     PA_GEOM_CASE(512, 8, 3)
   } else if constexpr (!HAS_VALS) {
     PA_GEOM_CASE(256, 12, 4)
