@@ -42,12 +42,13 @@ def main() -> None:
         keys = workloads.constant_u32(n)
     else:
         keys = workloads.uniform_u32(n)
-    dt = {4: torch.int32, 8: torch.int64}[keys.dtype.itemsize]
     src = torch.from_numpy(keys.view({4: np.int32, 8: np.int64}[keys.dtype.itemsize])).cuda()
     k = torch.empty_like(src)
     t = torch.empty_like(src)
-    v = torch.arange(n, dtype=torch.int32, device="cuda")
-    tv = torch.empty_like(v)
+    v = tv = None
+    if a.op == "sort_kv_u64":
+        v = torch.arange(n, dtype=torch.int32, device="cuda")
+        tv = torch.empty_like(v)
     out = torch.zeros(256, dtype=torch.int64, device="cuda")
     stream = torch.cuda.current_stream()
     o = _native.opts(stream.cuda_stream)
@@ -66,7 +67,6 @@ def main() -> None:
         elif a.op == "sum_u32":
             _native.call("pa_sum_u32", P(k.data_ptr()), n, P(out.data_ptr()), o)
     torch.cuda.synchronize()
-    del dt
     print(f"profile driver done: op={a.op} n={n} reps={a.reps}")
 
 
