@@ -107,6 +107,20 @@ enum { PA_KEY_U32 = 0, PA_KEY_U64 = 1, PA_KEY_F32 = 2 };
 int pa_sort_timed(int key_kind, void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t n,
                   float* phase_ms, int phase_cap, const pa_opts* opts);
 
+/* Allocation-free sort of 32-bit keys.  No counterpart in the reference.
+ * For callers that must not allocate GPU memory -- code inside a framework
+ * whose caching allocator owns all device memory, or latency-critical loops
+ * where cudaMalloc's device-wide synchronisation would stall other streams.
+ * Same result as pa_sort_u32, but keys and tmp (n keys each) must both be
+ * device memory of the current device, and n is at most 4,194,304: the call
+ * works in a fixed ~4 MiB scratch array compiled into the library (held by
+ * every GPU that loads it) instead of a workspace it allocates.  The first
+ * call on a device looks up that array's device address; make it before any
+ * stream capture.  All calls share the array: calls whose work overlaps on
+ * the GPU (other streams or threads) race, so issue them one at a time.
+ * Synchronous; returns PA_ERR_ARG for host buffers or n above the limit. */
+int pa_sort_u32_noalloc(uint32_t* keys, uint32_t* tmp, size_t n, const pa_opts* opts);
+
 /* ---- digit histograms ----------------------------------------------------
  * pa_hist_byte_components_u32: out[d * 256 + b] = number of keys in a[0, n)
  *   whose byte d (d = 0..3, least significant first) equals b, from one read.

@@ -36,6 +36,7 @@ SIGNATURES: dict[str, list] = {
     "pa_sort_kv_f32": [_P, _P, _P, _P, _SZ, _O],
     "pa_sort_two_phase_u32": [_P, _P, _SZ, _O],
     "pa_sort_timed": [ctypes.c_int, _P, _P, _P, _P, _SZ, _P, ctypes.c_int, _O],
+    "pa_sort_u32_noalloc": [_P, _P, _SZ, _O],
     "pa_hist_byte_components_u32": [_P, _SZ, _P, _O],
     "pa_hist_one_byte_u32": [_P, _SZ, _U, _P, _O],
     "pa_hist_u8": [_P, _SZ, _P, _O],

@@ -385,6 +385,8 @@ int sum_impl(const void* a, size_t n, int kb, uint64_t* out, const pa_opts* opts
 
 }  // namespace
 
+int record_error(int status, const char* message) { return set_error(status, "%s", message); }
+
 const DeviceInfo& device_info() {
   static DeviceInfo infos[64];
   int dev = 0;

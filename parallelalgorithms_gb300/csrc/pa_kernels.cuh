@@ -29,6 +29,10 @@ struct SortCtrl {
   uint32_t executed;
 };
 
+// Records `message` as the calling thread's pa_last_error_message() and
+// returns `status` (for entry points outside pa_capi.cu).
+int record_error(int status, const char* message);
+
 // Device properties the launchers size grids with (filled once per device).
 struct DeviceInfo {
   int device = -1;
