@@ -174,6 +174,40 @@ int pa_select_radix_u32(uint32_t* a, size_t start, size_t length, size_t k, uint
 int pa_sum_u32(const uint32_t* a, size_t n, uint64_t* out, const pa_opts* opts);
 int pa_sum_u64(const uint64_t* a, size_t n, uint64_t* out, const pa_opts* opts);
 
+/* ---- batched segmented sort -----------------------------------------------
+ * No reference counterpart (the reference sorts one array per call).  Sorts
+ * every segment [seg_offsets[i], seg_offsets[i + 1]) of one uint32 key array
+ * independently (stable, ascending; each segment's result equals
+ * pa_sort_u32 on it) in ONE persistent kernel launch fed by a device work
+ * queue: segments up to `small_cutoff` keys are sorted inside one CTA's
+ * shared memory, longer ones by the onesweep passes.  A plan is built once
+ * for a segmentation and replayed (through a captured CUDA graph when
+ * use_graph is set); pa_segmented_sort_u32 is the one-shot form.  Segments
+ * must be shorter than 2^30 keys.
+ */
+typedef struct pa_segsort_config {
+  int small_cutoff;  /* 0 (= 4096), 2048, 4096 or 8192 keys */
+  int tile_keys;     /* onesweep tile for longer segments: 0 (= 8192), 4096 or 8192 */
+  int digit_bits;    /* 0 or 8 */
+  int use_graph;     /* 1: plan runs replay a captured CUDA graph */
+  int reserved[4];   /* must be zero */
+} pa_segsort_config;
+typedef struct pa_segsort_plan pa_segsort_plan;
+
+/* seg_offsets: num_segments + 1 non-decreasing offsets (host or device). */
+int pa_segsort_plan_create(const uint64_t* seg_offsets, size_t num_segments, const pa_segsort_config* cfg,
+                           pa_segsort_plan** plan);
+/* keys, tmp: device buffers of the plan's total key count; sorted in keys.
+ * With opts->async_device the call returns after the launch; then
+ * pa_segsort_plan_sync(plan, stream) waits and reports bounded-wait failures. */
+int pa_segsort_plan_run(pa_segsort_plan* plan, uint32_t* keys, uint32_t* tmp, const pa_opts* opts);
+int pa_segsort_plan_sync(pa_segsort_plan* plan, void* stream);
+int pa_segsort_plan_info(const pa_segsort_plan* plan, uint32_t* num_small, uint32_t* num_large, uint32_t* num_items);
+int pa_segsort_plan_destroy(pa_segsort_plan* plan);
+/* One-shot: keys may be host or device memory. */
+int pa_segmented_sort_u32(uint32_t* keys, const uint64_t* seg_offsets, size_t num_segments,
+                          const pa_segsort_config* cfg, const pa_opts* opts);
+
 #ifdef __cplusplus
 }
 #endif

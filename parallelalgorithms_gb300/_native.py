@@ -21,6 +21,11 @@ class PaOpts(ctypes.Structure):
                 ("reserved", ctypes.c_int * 4)]
 
 
+class SegSortConfig(ctypes.Structure):
+    _fields_ = [("small_cutoff", ctypes.c_int), ("tile_keys", ctypes.c_int), ("digit_bits", ctypes.c_int),
+                ("use_graph", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+
+
 _P = ctypes.c_void_p
 _SZ = ctypes.c_size_t
 _U = ctypes.c_uint
@@ -47,6 +52,12 @@ SIGNATURES: dict[str, list] = {
     "pa_select_radix_u32": [_P, _SZ, _SZ, _SZ, _P, _O],
     "pa_sum_u32": [_P, _SZ, _P, _O],
     "pa_sum_u64": [_P, _SZ, _P, _O],
+    "pa_segsort_plan_create": [_P, _SZ, ctypes.POINTER(SegSortConfig), ctypes.POINTER(ctypes.c_void_p)],
+    "pa_segsort_plan_run": [_P, _P, _P, _O],
+    "pa_segsort_plan_sync": [_P, _P],
+    "pa_segsort_plan_info": [_P, _P, _P, _P],
+    "pa_segsort_plan_destroy": [_P],
+    "pa_segmented_sort_u32": [_P, _P, _SZ, ctypes.POINTER(SegSortConfig), _O],
     "pa_stream_check": [_P],
     "pa_device_available": [],
     "pa_release_workspaces": [],

@@ -99,6 +99,12 @@ __device__ __forceinline__ void st_relaxed_gpu(unsigned long long* p, unsigned l
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 // ---------------------------------------------------------------------------
 // mbarrier + bulk copy (the TMA engine's non-tensor form: a contiguous run of
 // bytes, 16-byte aligned on both sides, size a multiple of 16).
@@ -144,6 +150,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   raise_error(err, DEVERR_TMA_TIMEOUT);
   return false;
 }
+
+// Orders this thread's earlier (generic-proxy) view of global memory before
+// its later bulk copies (async proxy): needed when the data a bulk copy reads
+// was written by other CTAs of the same launch and published to this thread
+// through an acquire.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async;" ::: "memory"); }
 
 // Global -> shared bulk copy completing on `bar` (complete_tx counts bytes).
 __device__ __forceinline__ void bulk_load_g2s(void* smem_dst, const void* gmem_src, uint32_t bytes, uint64_t* bar) {

@@ -1,0 +1,580 @@
+// Batched segmented sort: thousands of uint32 arrays of uneven size, each
+// sorted independently (stable, ascending), in ONE persistent kernel launch
+// fed by a device work queue, launched through a captured CUDA graph.
+//
+// No reference counterpart: the reference sorts one array per call
+// (SortRadixPar, RadixSortLsdParallel.h:367); its nearest idea is bundling
+// small work items (BundleSmallWorkItems.cpp:36).  Per segment the result is
+// exactly SortRadixPar's.
+//
+// Work items, in queue order (a CTA takes the next item with one atomicAdd):
+//   HIST  one chunk of a large segment: its four byte-digit counts, added
+//         into the segment's histogram;
+//   SCAN  one large segment: bin starts of its four digits;
+//   PASS  one tile of one large segment for digit pass p: the onesweep tile
+//         of the plain sort (pa_onesweep_tile.cuh), look-back within the
+//         segment;
+//   SMALL one small segment (<= the small/large cutoff) sorted entirely in
+//         shared memory by eight stable 4-bit counting passes, read once and
+//         written once.
+// Small items are spread between the large-segment stages so that CTAs
+// waiting on a stage have work.  An item waits only on earlier items of the
+// same segment (per-segment completion counters: HIST chunks before SCAN,
+// SCAN before pass 0, all tiles of pass p before pass p + 1); items are taken
+// in queue order by running CTAs, so the earliest unfinished item can always
+// proceed.  Every wait is bounded and reports through the plan's error word.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "pa_common.cuh"
+#include "pa_gpu.h"
+#include "pa_kernels.cuh"
+#include "pa_onesweep_tile.cuh"
+
+namespace pa {
+namespace seg {
+
+using namespace os;
+
+constexpr int kBlock = 512;
+constexpr int kPasses = 4;                  // uint32 keys, 8-bit digits
+constexpr uint32_t kHistChunk = 64 * 1024;  // keys per HIST item
+constexpr int kHistLanes = 8;               // lane-banked copies of each counter
+constexpr uint32_t kMaxSegmentKeys = (1u << 30) - 1;  // 32-bit look-back words
+
+enum : uint32_t { ITEM_SMALL = 0, ITEM_HIST = 1, ITEM_SCAN = 2, ITEM_PASS = 3 };
+enum : uint32_t { ST_HIST = 0, ST_SCAN = 1, ST_PASS0 = 2, kStages = 2 + kPasses };
+
+struct Item {
+  uint32_t kind;
+  uint32_t pass;
+  uint32_t seg;  // segment index (SMALL) or large-segment index
+  uint32_t idx;  // tile (PASS) or chunk (HIST)
+};
+
+struct LargeSeg {
+  unsigned long long base;
+  uint32_t len;
+  uint32_t tiles;
+  uint32_t hist_chunks;
+  uint32_t tile_base;  // first tile of this segment in each pass's status array
+};
+
+struct PlanDev {
+  uint32_t* keys;
+  uint32_t* tmp;
+  const Item* items;
+  uint32_t num_items;
+  uint32_t total_tiles;
+  const unsigned long long* seg_off;
+  const LargeSeg* large;
+  uint32_t* head;                  // zeroed per run
+  uint32_t* done;                  // [large][kStages], zeroed per run
+  uint32_t* hist;                  // [large][4][256], zeroed per run
+  uint32_t* status;                // [kPasses][total_tiles][256], zeroed per run
+  unsigned long long* bin_start;   // [large][4][256]
+  uint32_t* err;
+};
+
+// Bounded wait until *ctr >= need (acquire).  Thread 0 only.
+__device__ __forceinline__ void wait_count(const uint32_t* ctr, uint32_t need, uint32_t* err) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    if (ld_acquire_gpu(ctr) >= need) return;
+    __nanosleep(64);
+  }
+  raise_error(err, DEVERR_LOOKBACK_TIMEOUT);
+}
+
+__device__ __forceinline__ void hist_item(const PlanDev& P, const Item& it, unsigned char* smem) {
+  const LargeSeg L = P.large[it.seg];
+  uint32_t* h = reinterpret_cast<uint32_t*>(smem);
+  constexpr uint32_t kWords = 4 * 256 * kHistLanes;
+  for (uint32_t i = threadIdx.x; i < kWords; i += kBlock) h[i] = 0;
+  __syncthreads();
+  const uint32_t lo = it.idx * kHistChunk;
+  const uint32_t len = min(kHistChunk, L.len - lo);
+  const uint32_t* src = P.keys + L.base + lo;
+  uint32_t* my = h + (threadIdx.x % kHistLanes);
+  for (uint32_t i = threadIdx.x; i < len; i += kBlock) {
+    const uint32_t k = src[i];
+#pragma unroll
+    for (int d = 0; d < 4; ++d) atomicAdd(my + ((uint32_t)d * 256 + ((k >> (8 * d)) & 255u)) * kHistLanes, 1u);
+  }
+  __syncthreads();
+  for (uint32_t e = threadIdx.x; e < 4 * 256; e += kBlock) {
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < kHistLanes; ++j) sum += h[e * kHistLanes + ((j + e) % kHistLanes)];
+    if (sum) atomicAdd(&P.hist[(size_t)it.seg * 1024 + e], sum);
+  }
+}
+
+__device__ __forceinline__ void scan_item(const PlanDev& P, const Item& it, unsigned char* smem) {
+  uint32_t* s_warp = reinterpret_cast<uint32_t*>(smem);
+  const uint32_t tid = threadIdx.x;
+  for (int d = 0; d < 4; ++d) {
+    const uint32_t c = tid < 256 ? P.hist[(size_t)it.seg * 1024 + d * 256 + tid] : 0u;
+    const uint32_t x = block_exclusive_scan<kBlock>(c, s_warp);
+    if (tid < 256) P.bin_start[(size_t)it.seg * 1024 + d * 256 + tid] = x;
+    __syncthreads();  // s_warp is reused by the next digit's scan
+  }
+}
+
+template <int PASS_ITEMS>
+__device__ __forceinline__ void pass_item(const PlanDev& P, const Item& it, unsigned char* smem, uint32_t& parity) {
+  const LargeSeg L = P.large[it.seg];
+  const bool even = (it.pass & 1u) == 0;
+  TileJob<uint32_t, uint32_t> job;
+  job.in = (even ? P.keys : P.tmp) + L.base;
+  job.out = (even ? P.tmp : P.keys) + L.base;
+  job.vin = nullptr;
+  job.vout = nullptr;
+  job.n = L.len;
+  job.tile = it.idx;
+  job.shift = 8u * it.pass;
+  job.tin = false;
+  job.tout = false;
+  job.bin_start = P.bin_start + (size_t)it.seg * 1024 + it.pass * 256;
+  job.status = P.status + ((size_t)it.pass * P.total_tiles + L.tile_base) * 256;
+  job.err = P.err;
+  onesweep_tile<uint32_t, false, kBlock, PASS_ITEMS, uint32_t>(job, smem, parity);
+}
+
+template <int SMALL_ITEMS>
+__device__ __forceinline__ void small_item(const PlanDev& P, const Item& it, unsigned char* smem) {
+  using GS = Geometry<uint32_t, false, kBlock, SMALL_ITEMS>;
+  constexpr uint32_t TILE = GS::kTile;
+  uint32_t* s_keys = reinterpret_cast<uint32_t*>(smem + GS::kKeysOff);
+  uint32_t* s_cnt = reinterpret_cast<uint32_t*>(smem + GS::kCntOff);
+  uint32_t* s_warp = reinterpret_cast<uint32_t*>(smem + GS::kWarpTotOff);
+  const unsigned long long base = P.seg_off[it.seg];
+  const uint32_t len = (uint32_t)(P.seg_off[it.seg + 1] - base);
+  uint32_t* keys = P.keys + base;
+  for (uint32_t i = threadIdx.x; i < TILE; i += kBlock) s_keys[i] = i < len ? keys[i] : 0xFFFFFFFFu;
+  __syncthreads();
+  uint32_t k[SMALL_ITEMS];
+  uint32_t v[1];
+#pragma unroll 1
+  for (uint32_t sh = 0; sh < 32; sh += 4) {
+    load_run<uint32_t, false, SMALL_ITEMS>(k, v, s_keys, nullptr);
+    nibble_pass<uint32_t, false, kBlock, SMALL_ITEMS>(k, v, sh, s_keys, nullptr, s_cnt, s_warp);
+  }
+  for (uint32_t i = threadIdx.x; i < len; i += kBlock) keys[i] = s_keys[i];
+}
+
+template <int PASS_ITEMS, int SMALL_ITEMS>
+__global__ void __launch_bounds__(kBlock, 2) segsort_kernel(const PlanDev P) {
+  using GP = Geometry<uint32_t, false, kBlock, PASS_ITEMS>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ Item s_item;
+  __shared__ uint32_t s_index;
+  uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + GP::kBarOff);
+  if (threadIdx.x == 0) {
+    mbar_init(s_bar, 1);
+    mbar_fence_init();
+  }
+  uint32_t parity = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const uint32_t i = atomicAdd(P.head, 1u);
+      s_index = i;
+      if (i < P.num_items) s_item = P.items[i];
+    }
+    __syncthreads();
+    if (s_index >= P.num_items) break;
+    const Item it = s_item;
+    if (it.kind == ITEM_SCAN || it.kind == ITEM_PASS) {
+      if (threadIdx.x == 0) {
+        const LargeSeg L = P.large[it.seg];
+        const uint32_t* d = P.done + (size_t)it.seg * kStages;
+        if (it.kind == ITEM_SCAN)
+          wait_count(d + ST_HIST, L.hist_chunks, P.err);
+        else if (it.pass == 0)
+          wait_count(d + ST_SCAN, 1, P.err);
+        else
+          wait_count(d + ST_PASS0 + it.pass - 1, L.tiles, P.err);
+        fence_proxy_async();
+      }
+      __syncthreads();
+    }
+    if (it.kind == ITEM_SMALL)
+      small_item<SMALL_ITEMS>(P, it, smem);
+    else if (it.kind == ITEM_HIST)
+      hist_item(P, it, smem);
+    else if (it.kind == ITEM_SCAN)
+      scan_item(P, it, smem);
+    else
+      pass_item<PASS_ITEMS>(P, it, smem, parity);
+    __syncthreads();
+    if (it.kind != ITEM_SMALL && threadIdx.x == 0) {
+      __threadfence();
+      const uint32_t st = it.kind == ITEM_HIST ? ST_HIST : it.kind == ITEM_SCAN ? ST_SCAN : ST_PASS0 + it.pass;
+      atomicAdd(P.done + (size_t)it.seg * kStages + st, 1u);
+    }
+  }
+}
+
+// ---- host side ---------------------------------------------------------------
+using KernelFn = void (*)(const PlanDev);
+
+template <int PI, int SI>
+constexpr size_t smem_bytes_for() {
+  using GP = Geometry<uint32_t, false, kBlock, PI>;
+  using GS = Geometry<uint32_t, false, kBlock, SI>;
+  size_t b = GP::kBytes;
+  if (GS::kBytes > b) b = GS::kBytes;
+  if ((size_t)4 * 256 * kHistLanes * 4 > b) b = (size_t)4 * 256 * kHistLanes * 4;
+  return b;
+}
+
+struct KernelChoice {
+  KernelFn fn;
+  size_t smem;
+  uint32_t pass_tile;
+  uint32_t small_tile;
+};
+
+template <int PI, int SI>
+KernelChoice choice() {
+  return {segsort_kernel<PI, SI>, smem_bytes_for<PI, SI>(), (uint32_t)kBlock * PI, (uint32_t)kBlock * SI};
+}
+
+bool pick_kernel(int tile_keys, int small_cutoff, KernelChoice* out) {
+  const int pi = tile_keys == 4096 ? 8 : tile_keys == 8192 ? 16 : 0;
+  const int si = small_cutoff == 2048 ? 4 : small_cutoff == 4096 ? 8 : small_cutoff == 8192 ? 16 : 0;
+  if (!pi || !si) return false;
+  if (pi == 8 && si == 4) *out = choice<8, 4>();
+  if (pi == 8 && si == 8) *out = choice<8, 8>();
+  if (pi == 8 && si == 16) *out = choice<8, 16>();
+  if (pi == 16 && si == 4) *out = choice<16, 4>();
+  if (pi == 16 && si == 8) *out = choice<16, 8>();
+  if (pi == 16 && si == 16) *out = choice<16, 16>();
+  return true;
+}
+
+}  // namespace seg
+}  // namespace pa
+
+using namespace pa;
+using namespace pa::seg;
+
+struct pa_segsort_plan {
+  int device = -1;
+  size_t num_segments = 0;
+  unsigned long long total_keys = 0;
+  pa_segsort_config cfg{};
+  KernelChoice kc{};
+  unsigned grid = 0;
+  char* dev = nullptr;
+  size_t zero_off = 0, zero_bytes = 0;
+  PlanDev pd{};
+  uint32_t num_items = 0, num_small = 0, num_large = 0;
+  uint32_t* err_host = nullptr;
+  cudaStream_t cap_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint32_t* g_keys = nullptr;
+  uint32_t* g_tmp = nullptr;
+};
+
+namespace {
+
+int cfail(cudaError_t e, const char* what) {
+  char buf[256];
+  snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+  cudaGetLastError();
+  return record_error(e == cudaErrorMemoryAllocation ? PA_ERR_OOM : PA_ERR_CUDA, buf);
+}
+
+#define PA_SEG_CUDA(call)                                 \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cfail(e_, #call);       \
+  } while (0)
+
+bool dev_ptr(const void* p) {
+  cudaPointerAttributes at;
+  if (!p || cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  int d = 0;
+  cudaGetDevice(&d);
+  return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == d;
+}
+
+void destroy_graph(pa_segsort_plan* p) {
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = nullptr;
+  p->graph = nullptr;
+  p->g_keys = p->g_tmp = nullptr;
+}
+
+int enqueue(pa_segsort_plan* p, cudaStream_t s) {
+  PA_SEG_CUDA(cudaMemsetAsync(p->dev + p->zero_off, 0, p->zero_bytes, s));
+  if (p->num_items) {
+    p->kc.fn<<<p->grid, kBlock, p->kc.smem, s>>>(p->pd);
+    PA_SEG_CUDA(cudaGetLastError());
+  }
+  return PA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pa_segsort_plan_create(const uint64_t* seg_offsets, size_t num_segments, const pa_segsort_config* cfg,
+                           pa_segsort_plan** out) {
+  if (!out) return record_error(PA_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (!seg_offsets) return record_error(PA_ERR_ARG, "seg_offsets is NULL");
+  pa_segsort_config c{};
+  if (cfg) c = *cfg;
+  for (int r : c.reserved)
+    if (r) return record_error(PA_ERR_ARG, "pa_segsort_config.reserved must be zero");
+  if (c.small_cutoff == 0) c.small_cutoff = 4096;
+  if (c.tile_keys == 0) c.tile_keys = 8192;
+  if (c.digit_bits == 0) c.digit_bits = 8;
+  if (c.digit_bits != 8) return record_error(PA_ERR_ARG, "digit_bits must be 8 for the batched sort");
+  KernelChoice kc{};
+  if (!pick_kernel(c.tile_keys, c.small_cutoff, &kc))
+    return record_error(PA_ERR_ARG, "tile_keys must be 4096 or 8192 and small_cutoff 2048, 4096 or 8192");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return record_error(PA_ERR_NO_DEVICE, "no CUDA device");
+  }
+  // The offsets must be readable on the host to plan the work.
+  std::vector<uint64_t> off(num_segments + 1);
+  if (dev_ptr(seg_offsets)) {
+    PA_SEG_CUDA(cudaMemcpy(off.data(), seg_offsets, off.size() * 8, cudaMemcpyDeviceToHost));
+  } else {
+    std::memcpy(off.data(), seg_offsets, off.size() * 8);
+  }
+  for (size_t i = 0; i < num_segments; ++i) {
+    if (off[i + 1] < off[i]) return record_error(PA_ERR_ARG, "seg_offsets must be non-decreasing");
+    if (off[i + 1] - off[i] > kMaxSegmentKeys)
+      return record_error(PA_ERR_ARG, "a segment exceeds 2^30 - 1 keys (the batched sort's limit)");
+  }
+
+  // ---- classify segments and build the queue ----------------------------------
+  std::vector<uint32_t> small_ids;
+  std::vector<LargeSeg> large;
+  std::vector<uint32_t> large_seg_id;
+  uint32_t total_tiles = 0;
+  for (size_t i = 0; i < num_segments; ++i) {
+    const uint64_t len = off[i + 1] - off[i];
+    if (len <= 1) continue;
+    if (len <= (uint64_t)kc.small_tile && len <= (uint64_t)c.small_cutoff) {
+      small_ids.push_back((uint32_t)i);
+    } else {
+      LargeSeg L{};
+      L.base = off[i];
+      L.len = (uint32_t)len;
+      L.tiles = (uint32_t)((len + kc.pass_tile - 1) / kc.pass_tile);
+      L.hist_chunks = (uint32_t)((len + kHistChunk - 1) / kHistChunk);
+      L.tile_base = total_tiles;
+      total_tiles += L.tiles;
+      large.push_back(L);
+      large_seg_id.push_back((uint32_t)i);
+    }
+  }
+  // largest small segments first (they take longest)
+  std::stable_sort(small_ids.begin(), small_ids.end(),
+                   [&](uint32_t a, uint32_t b) { return off[a + 1] - off[a] > off[b + 1] - off[b]; });
+  std::vector<Item> items;
+  size_t next_small = 0;
+  const size_t gaps = 1 + 1 + kPasses;  // after HIST, SCAN, and each pass but the last
+  auto add_small = [&](size_t share_of) {
+    const size_t upto = std::min(small_ids.size(), (small_ids.size() * share_of + gaps - 1) / gaps);
+    for (; next_small < upto; ++next_small) items.push_back({ITEM_SMALL, 0, small_ids[next_small], 0});
+  };
+  for (uint32_t l = 0; l < large.size(); ++l)
+    for (uint32_t ch = 0; ch < large[l].hist_chunks; ++ch) items.push_back({ITEM_HIST, 0, l, ch});
+  add_small(1);
+  for (uint32_t l = 0; l < large.size(); ++l) items.push_back({ITEM_SCAN, 0, l, 0});
+  add_small(2);
+  for (uint32_t p = 0; p < (uint32_t)kPasses; ++p) {
+    for (uint32_t l = 0; l < large.size(); ++l)
+      for (uint32_t t = 0; t < large[l].tiles; ++t) items.push_back({ITEM_PASS, p, l, t});
+    add_small(3 + p);
+  }
+  add_small(gaps);
+
+  // ---- device memory ------------------------------------------------------------
+  auto* p = new pa_segsort_plan();
+  cudaGetDevice(&p->device);
+  p->num_segments = num_segments;
+  p->total_keys = num_segments ? off[num_segments] : 0;
+  p->cfg = c;
+  p->kc = kc;
+  p->num_items = (uint32_t)items.size();
+  p->num_small = (uint32_t)small_ids.size();
+  p->num_large = (uint32_t)large.size();
+  const size_t nl = std::max<size_t>(large.size(), 1);
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    o = (o + 255) & ~(size_t)255;
+    const size_t at = o;
+    o += bytes;
+    return at;
+  };
+  const size_t o_items = take(std::max<size_t>(items.size(), 1) * sizeof(Item));
+  const size_t o_off = take(off.size() * 8);
+  const size_t o_large = take(nl * sizeof(LargeSeg));
+  const size_t o_bins = take(nl * 1024 * 8);
+  const size_t o_err = take(256);
+  const size_t o_head = take(256);
+  const size_t o_done = take(nl * kStages * 4);
+  const size_t o_hist = take(nl * 1024 * 4);
+  const size_t o_status = take((size_t)kPasses * std::max<uint32_t>(total_tiles, 1) * 256 * 4);
+  const size_t total = o;
+  cudaError_t e = cudaMalloc(&p->dev, total);
+  if (e != cudaSuccess) {
+    delete p;
+    return cfail(e, "cudaMalloc(plan)");
+  }
+  e = cudaMallocHost(&p->err_host, sizeof(uint32_t));
+  if (e == cudaSuccess && !items.empty())
+    e = cudaMemcpy(p->dev + o_items, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->dev + o_off, off.data(), off.size() * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !large.empty())
+    e = cudaMemcpy(p->dev + o_large, large.data(), large.size() * sizeof(LargeSeg), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(p->dev + o_err, 0, 256);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kc.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kc.smem);
+  int per_sm = 0;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kc.fn, kBlock, kc.smem);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    pa_segsort_plan_destroy(p);
+    return cfail(e, "plan set-up");
+  }
+  p->grid = (unsigned)std::max(1, per_sm) * (unsigned)device_info().sm_count;
+  if (p->num_items < p->grid) p->grid = std::max<uint32_t>(p->num_items, 1);
+  p->zero_off = o_head;
+  p->zero_bytes = total - o_head;
+  PlanDev& d = p->pd;
+  d.items = reinterpret_cast<const Item*>(p->dev + o_items);
+  d.num_items = p->num_items;
+  d.total_tiles = total_tiles;
+  d.seg_off = reinterpret_cast<const unsigned long long*>(p->dev + o_off);
+  d.large = reinterpret_cast<const LargeSeg*>(p->dev + o_large);
+  d.head = reinterpret_cast<uint32_t*>(p->dev + o_head);
+  d.done = reinterpret_cast<uint32_t*>(p->dev + o_done);
+  d.hist = reinterpret_cast<uint32_t*>(p->dev + o_hist);
+  d.status = reinterpret_cast<uint32_t*>(p->dev + o_status);
+  d.bin_start = reinterpret_cast<unsigned long long*>(p->dev + o_bins);
+  d.err = reinterpret_cast<uint32_t*>(p->dev + o_err);
+  *out = p;
+  return PA_OK;
+}
+
+int pa_segsort_plan_info(const pa_segsort_plan* p, uint32_t* num_small, uint32_t* num_large, uint32_t* num_items) {
+  if (!p) return record_error(PA_ERR_ARG, "plan is NULL");
+  if (num_small) *num_small = p->num_small;
+  if (num_large) *num_large = p->num_large;
+  if (num_items) *num_items = p->num_items;
+  return PA_OK;
+}
+
+int pa_segsort_plan_run(pa_segsort_plan* p, uint32_t* keys, uint32_t* tmp, const pa_opts* opts) {
+  if (!p) return record_error(PA_ERR_ARG, "plan is NULL");
+  if (p->total_keys == 0) return PA_OK;
+  if (!dev_ptr(keys) || !dev_ptr(tmp))
+    return record_error(PA_ERR_ARG, "keys and tmp must be device memory holding the plan's total key count");
+  cudaStream_t s = opts ? static_cast<cudaStream_t>(opts->stream) : (cudaStream_t)0;
+  p->pd.keys = keys;
+  p->pd.tmp = tmp;
+  if (p->cfg.use_graph) {
+    if (!p->exec || p->g_keys != keys || p->g_tmp != tmp) {
+      destroy_graph(p);
+      PA_SEG_CUDA(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
+      const int rc = enqueue(p, p->cap_stream);
+      cudaGraph_t g = nullptr;
+      const cudaError_t ec = cudaStreamEndCapture(p->cap_stream, &g);
+      if (rc != PA_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (ec != cudaSuccess) return cfail(ec, "cudaStreamEndCapture");
+      p->graph = g;
+      PA_SEG_CUDA(cudaGraphInstantiate(&p->exec, p->graph, 0));
+      p->g_keys = keys;
+      p->g_tmp = tmp;
+    }
+    PA_SEG_CUDA(cudaGraphLaunch(p->exec, s));
+  } else {
+    if (int rc = enqueue(p, s)) return rc;
+  }
+  if (opts && opts->async_device) return PA_OK;
+  return pa_segsort_plan_sync(p, opts ? opts->stream : nullptr);
+}
+
+int pa_segsort_plan_sync(pa_segsort_plan* p, void* stream) {
+  if (!p) return record_error(PA_ERR_ARG, "plan is NULL");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  PA_SEG_CUDA(cudaMemcpyAsync(p->err_host, p->pd.err, 4, cudaMemcpyDeviceToHost, s));
+  PA_SEG_CUDA(cudaStreamSynchronize(s));
+  if (*p->err_host) {
+    PA_SEG_CUDA(cudaMemsetAsync(p->pd.err, 0, 4, s));
+    PA_SEG_CUDA(cudaStreamSynchronize(s));
+    return record_error(PA_ERR_TIMEOUT, "a bounded device-side wait of the batched sort gave up");
+  }
+  return PA_OK;
+}
+
+int pa_segsort_plan_destroy(pa_segsort_plan* p) {
+  if (!p) return PA_OK;
+  destroy_graph(p);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  if (p->dev) cudaFree(p->dev);
+  if (p->err_host) cudaFreeHost(p->err_host);
+  delete p;
+  return PA_OK;
+}
+
+int pa_segmented_sort_u32(uint32_t* keys, const uint64_t* seg_offsets, size_t num_segments,
+                          const pa_segsort_config* cfg, const pa_opts* opts) {
+  if (num_segments == 0) return PA_OK;
+  if (!keys || !seg_offsets) return record_error(PA_ERR_ARG, "NULL buffer");
+  pa_segsort_plan* p = nullptr;
+  pa_segsort_config c{};
+  if (cfg) c = *cfg;
+  c.use_graph = 0;  // one-shot: nothing to replay
+  if (int rc = pa_segsort_plan_create(seg_offsets, num_segments, &c, &p)) return rc;
+  const size_t n = (size_t)p->total_keys;
+  cudaStream_t s = opts ? static_cast<cudaStream_t>(opts->stream) : (cudaStream_t)0;
+  uint32_t* d_keys = keys;
+  uint32_t* d_tmp = nullptr;
+  const bool host = !dev_ptr(keys);
+  cudaError_t e = cudaSuccess;
+  if (n && host) e = cudaMalloc(&d_keys, n * 4);
+  if (e == cudaSuccess && n) e = cudaMalloc(&d_tmp, n * 4);
+  if (e == cudaSuccess && n && host) e = cudaMemcpyAsync(d_keys, keys, n * 4, cudaMemcpyHostToDevice, s);
+  int rc = PA_OK;
+  if (e != cudaSuccess) {
+    rc = cfail(e, "batched sort buffers");
+  } else if (n) {
+    pa_opts o{};
+    if (opts) o = *opts;
+    o.async_device = 0;
+    rc = pa_segsort_plan_run(p, d_keys, d_tmp, &o);
+    if (rc == PA_OK && host) {
+      e = cudaMemcpyAsync(keys, d_keys, n * 4, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) rc = cfail(e, "copy back");
+    }
+  }
+  if (d_tmp) cudaFree(d_tmp);
+  if (host && d_keys && d_keys != keys) cudaFree(d_keys);
+  pa_segsort_plan_destroy(p);
+  return rc;
+}
+
+}  // extern "C"
