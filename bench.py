@@ -375,6 +375,78 @@ def _time_device(fn, reps: int, stream, restore=None) -> float:
     return statistics.median(ts)
 
 
+def batched_extra(lib, _native, workloads, stream, peak) -> dict:
+    """4096 uint32 arrays, sizes log-uniform in [1e3, 4e6] (seed 1238), ~200M
+    keys: one batched plan (autotuned, CUDA graph) vs one pa_sort_u32 per array."""
+    import torch
+
+    from parallelalgorithms_gb300 import batched
+    P = ctypes.c_void_p
+    sizes = workloads.log_uniform_sizes(4096, 1e3, 4e6)
+    off = np.zeros(sizes.size + 1, np.uint64)
+    off[1:] = np.cumsum(sizes)
+    total = int(off[-1])
+    keys = workloads.uniform_u32(total, seed=workloads.SEED_SEGMENT_SIZES)
+    src = torch.from_numpy(keys.view(np.int32)).cuda()
+    d = src.clone()
+    t = torch.empty_like(src)
+    tune = batched.autotune(off, d, t, reps=2)
+    choice = tune["choice"]
+    plan = batched.SegmentedSortPlan(off, choice, use_graph=True)
+    info = plan.info()
+    times = []
+    for r in range(6):
+        d.copy_(src)
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        plan.run(d, t, stream.cuda_stream, sync=False)
+        e.record(stream)
+        plan.sync(stream.cuda_stream)
+        if r:
+            times.append(s.elapsed_time(e))
+    ms = statistics.median(times)
+    # sorted within every segment (order-preserving int32 view: flip the sign bit)
+    f = d ^ torch.tensor(-2147483648, dtype=torch.int32, device=d.device)
+    ok = f[1:] >= f[:-1]
+    bounds = torch.from_numpy(off[1:-1].astype(np.int64) - 1).cuda()
+    ok[bounds[(bounds >= 0) & (bounds < ok.numel())]] = True
+    sorted_ok = bool(torch.all(ok))
+    del f, ok
+    # the same arrays, one plain sort call per array
+    o = _native.opts(stream.cuda_stream, async_device=True)
+    d.copy_(src)
+    torch.cuda.synchronize()
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    s.record(stream)
+    base = d.data_ptr()
+    tbase = t.data_ptr()
+    for i in range(sizes.size):
+        a = int(off[i])
+        _native.call("pa_sort_u32", P(base + 4 * a), P(tbase + 4 * a), int(sizes[i]), o)
+    e.record(stream)
+    torch.cuda.synchronize()
+    wall_plain = (time.perf_counter() - t0) * 1e3
+    _native.call("pa_stream_check", P(stream.cuda_stream))
+    plain_ms = s.elapsed_time(e)
+    small = sizes <= choice.small_cutoff
+    model_bytes = float(8 * sizes[small].sum() + 36 * sizes[~small].sum())
+    plan.close()
+    del src, d, t
+    torch.cuda.empty_cache()
+    return {"segments": int(sizes.size), "keys": total, "ms": ms, "keys_per_s": total / (ms / 1e3),
+            "sorted_within_segments": sorted_ok,
+            "choice": {"small_cutoff": choice.small_cutoff, "tile_keys": choice.tile_keys,
+                       "digit_bits": choice.digit_bits},
+            "autotune_ms": tune["ms"], "plan": info, "graph": True,
+            "plain_per_array_ms": plain_ms, "plain_per_array_wall_ms": wall_plain,
+            "speedup_vs_plain_per_array": plain_ms / ms,
+            "bytes_model": "8 B/key for shared-memory segments, 36 B/key for onesweep segments",
+            "achieved_gbs": model_bytes / (ms / 1e3) / 1e9, "frac": model_bytes / (ms / 1e3) / 1e9 / peak}
+
+
 def run_extras(pa, lib, _native, workloads, n, stream, peak) -> dict:
     """Other 100M workloads of the same path, device-resident, median of 5."""
     import torch
@@ -441,6 +513,7 @@ def run_extras(pa, lib, _native, workloads, n, stream, peak) -> dict:
                                    "frac": 4 * n / (ms / 1e3) / 1e9 / peak}
         _native.call("pa_stream_check", P(stream.cuda_stream))
         del d
+    out["batched_segmented_sort_4096_arrays"] = batched_extra(lib, _native, workloads, stream, peak)
     return out
 
 

@@ -61,3 +61,24 @@ def test_f32_100m_total_order(pa, port):
     wk, wv = port.sort(a, vals)
     np.testing.assert_array_equal(k.view(np.uint32), wk.view(np.uint32))
     np.testing.assert_array_equal(v, wv)
+
+
+def test_batched_4096_arrays_200m(pa, port, torch_cuda):
+    """4096 arrays, sizes log-uniform in [1e3, 4e6] (~200M keys), one plan,
+    bit-exact per segment against the oracle."""
+    from parallelalgorithms_gb300 import batched, workloads
+    torch = torch_cuda
+    sizes = workloads.log_uniform_sizes(4096, 1e3, 4e6)
+    off = np.zeros(sizes.size + 1, np.uint64)
+    off[1:] = np.cumsum(sizes)
+    keys = workloads.uniform_u32(int(off[-1]), seed=workloads.SEED_SEGMENT_SIZES)
+    d = torch.from_numpy(keys.view(np.int32).copy()).cuda()
+    t = torch.empty_like(d)
+    plan = batched.SegmentedSortPlan(off)
+    plan.run(d, t)
+    got = d.cpu().numpy().view(np.uint32)
+    for i in range(sizes.size):
+        a, b = int(off[i]), int(off[i + 1])
+        want, _ = port.sort(keys[a:b])
+        np.testing.assert_array_equal(got[a:b], want, err_msg=f"segment {i}")
+    plan.close()
