@@ -208,6 +208,58 @@ int pa_segsort_plan_destroy(pa_segsort_plan* plan);
 int pa_segmented_sort_u32(uint32_t* keys, const uint64_t* seg_offsets, size_t num_segments,
                           const pa_segsort_config* cfg, const pa_opts* opts);
 
+/* ---- serving loop ----------------------------------------------------------
+ * No reference counterpart.  A server takes sort / select / histogram
+ * requests from any thread as they arrive, admits them while their device
+ * memory fits a configured HBM budget (and the memory the GPU reports free),
+ * keeps their data device-resident while they run, overlaps requests on
+ * several streams, and coalesces waiting 32-bit sorts into one batched
+ * launch.  Results equal the plain entry points' (pa_sort_*, pa_select_*,
+ * pa_hist_one_byte_*) on the same request.  Host buffers should be pinned
+ * for copies to overlap; device buffers are used in place (sort) or read.
+ */
+enum { PA_REQ_SORT = 0, PA_REQ_SELECT = 1, PA_REQ_HISTOGRAM = 2 };
+
+typedef struct pa_request {
+  int op;            /* PA_REQ_SORT, PA_REQ_SELECT or PA_REQ_HISTOGRAM */
+  int key_kind;      /* PA_KEY_U32 or PA_KEY_U64 */
+  void* keys;        /* n keys (host or device); a sort leaves them sorted here */
+  size_t n;
+  uint64_t k;        /* select: 0-based rank */
+  unsigned shift;    /* histogram: counts of (key >> shift) & 255 */
+  uint64_t* result;  /* select: 1 word (the key, zero-extended); histogram: 256 counts (host) */
+  int status;        /* written by the server: -1 while pending, then a pa_status */
+  int unit_size;     /* written by the server: requests that shared its launch (1 = alone) */
+  double t_submit, t_admit, t_done;  /* written by the server: seconds, monotonic clock */
+  int internal_device;               /* written by the server */
+} pa_request;
+
+typedef struct pa_serve_config {
+  size_t hbm_budget_bytes;  /* device memory the server may hold: 0 = 64 GiB */
+  int max_inflight;         /* units on the device at once: 0 = 4 */
+  int max_batch_requests;   /* 32-bit sorts coalesced into one launch: 0 = 256 */
+  int no_coalesce;          /* 1: every request runs alone */
+  int num_streams;          /* 0 = 4 */
+  int reserved[4];          /* must be zero */
+} pa_serve_config;
+typedef struct pa_server pa_server;
+
+int pa_server_create(const pa_serve_config* cfg, pa_server** server);
+/* Non-blocking; the request must stay alive until it completes. */
+int pa_server_submit(pa_server* server, pa_request* req);
+/* Blocks until the request completes; returns its status. */
+int pa_server_wait(pa_server* server, pa_request* req);
+/* Blocks until every submitted request has completed. */
+int pa_server_drain(pa_server* server);
+/* out[0..6] = submitted, completed, rejected (over budget), units launched,
+ * batched units, requests served in batches, peak device bytes held. */
+int pa_server_stats(pa_server* server, uint64_t* out, int count);
+int pa_server_destroy(pa_server* server);
+
+/* 256-bin histogram of (key >> shift) & 255 over 64-bit keys (no reference
+ * counterpart; the 32-bit form is pa_hist_one_byte_u32). shift < 64. */
+int pa_hist_one_byte_u64(const uint64_t* a, size_t n, unsigned shift, uint64_t* out, const pa_opts* opts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,13 @@ SIGNATURES: dict[str, list] = {
     "pa_segsort_plan_info": [_P, _P, _P, _P],
     "pa_segsort_plan_destroy": [_P],
     "pa_segmented_sort_u32": [_P, _P, _SZ, ctypes.POINTER(SegSortConfig), _O],
+    "pa_server_create": [_P, ctypes.POINTER(ctypes.c_void_p)],
+    "pa_server_submit": [_P, _P],
+    "pa_server_wait": [_P, _P],
+    "pa_server_drain": [_P],
+    "pa_server_stats": [_P, _P, ctypes.c_int],
+    "pa_server_destroy": [_P],
+    "pa_hist_one_byte_u64": [_P, _SZ, _U, _P, _O],
     "pa_stream_check": [_P],
     "pa_device_available": [],
     "pa_release_workspaces": [],

@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -21,6 +22,20 @@
 #include "pa_kernels.cuh"
 
 namespace pa {
+
+// Lays out sub-buffers in one allocation, 256-byte aligned.  Run once with
+// base == nullptr to measure, then with the real base.
+struct Carve {
+  char* base;
+  size_t off = 0;
+  template <class T>
+  T* take(size_t count) {
+    off = (off + 255) & ~(size_t)255;
+    T* p = reinterpret_cast<T*>(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+};
 
 namespace {
 
@@ -62,20 +77,6 @@ struct Workspace {
 
 std::mutex g_mu;
 std::map<std::pair<int, cudaStream_t>, Workspace> g_ws;
-
-// Lays out sub-buffers in one allocation, 256-byte aligned.  Run once with
-// base == nullptr to measure, then with the real base.
-struct Carve {
-  char* base;
-  size_t off = 0;
-  template <class T>
-  T* take(size_t count) {
-    off = (off + 255) & ~(size_t)255;
-    T* p = reinterpret_cast<T*>(base + off);
-    off += count * sizeof(T);
-    return p;
-  }
-};
 
 int device_ready() {
   int count = 0;
@@ -183,35 +184,18 @@ int sort_impl(void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t 
   const bool tmp_dev = is_device_ptr(tmp);
   const bool vals_dev = has_vals && is_device_ptr(vals);
   const bool tvals_dev = has_vals && is_device_ptr(tmp_vals);
-  const int passes = kb;  // 8-bit digits: one pass per key byte
-  const size_t tile = onesweep_tile_keys(kb, has_vals);
-  const size_t tiles = ceil_div(n, tile);
-  const size_t sb = onesweep_status_bytes(n);
-
-  struct Layout {
-    void *d_keys, *d_tmp;
-    uint32_t *d_vals, *d_tvals;
-    unsigned long long* counts;
-    uint32_t* tile_ctr;
-    char* status;
-    unsigned long long* bin_start;
-    SortCtrl* ctrl;
-    size_t zero_off, zero_bytes;
-  } L{};
+  void *d_keys = nullptr, *d_tmp = nullptr;
+  uint32_t *d_vals = nullptr, *d_tvals = nullptr;
+  SortScratch sc{};
   auto layout = [&](Carve& c) {
-    L.d_keys = keys_dev ? keys : c.take<char>(n * kb);
-    L.d_tmp = tmp_dev ? tmp : c.take<char>(n * kb);
+    d_keys = keys_dev ? keys : c.take<char>(n * kb);
+    d_tmp = tmp_dev ? tmp : c.take<char>(n * kb);
     if (has_vals) {
-      L.d_vals = vals_dev ? vals : c.take<uint32_t>(n);
-      L.d_tvals = tvals_dev ? tmp_vals : c.take<uint32_t>(n);
+      d_vals = vals_dev ? vals : c.take<uint32_t>(n);
+      d_tvals = tvals_dev ? tmp_vals : c.take<uint32_t>(n);
     }
-    L.counts = c.take<unsigned long long>((size_t)passes * 256);
-    L.zero_off = (size_t)(reinterpret_cast<char*>(L.counts) - c.base);
-    L.tile_ctr = c.take<uint32_t>(passes);
-    L.status = c.take<char>((size_t)passes * tiles * 256 * sb);
-    L.zero_bytes = c.off - L.zero_off;
-    L.bin_start = c.take<unsigned long long>((size_t)passes * 256);
-    L.ctrl = c.take<SortCtrl>(1);
+    char* sbase = c.take<char>(sort_scratch_bytes(n, kb, has_vals));
+    sort_scratch_layout(sbase, n, kb, has_vals, &sc);
   };
   Carve measure{nullptr};
   layout(measure);
@@ -220,10 +204,9 @@ int sort_impl(void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t 
   layout(real);
 
   const size_t key_bytes_total = n * (size_t)kb;
-  if (!keys_dev) PA_CUDA(cudaMemcpyAsync(L.d_keys, keys, key_bytes_total, cudaMemcpyHostToDevice, stream));
+  if (!keys_dev) PA_CUDA(cudaMemcpyAsync(d_keys, keys, key_bytes_total, cudaMemcpyHostToDevice, stream));
   if (has_vals && !vals_dev)
-    PA_CUDA(cudaMemcpyAsync(L.d_vals, vals, n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
-  PA_CUDA(cudaMemsetAsync(ws->dev + L.zero_off, 0, L.zero_bytes, stream));
+    PA_CUDA(cudaMemcpyAsync(d_vals, vals, n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
   const bool timed = phase_ms && phase_cap > 0;
   int nev = 0;
   auto mark = [&]() -> cudaError_t {
@@ -234,34 +217,10 @@ int sort_impl(void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t 
     }
     return cudaEventRecord(ws->ev[nev++], stream);
   };
-  PA_CUDA(mark());
-  PA_CUDA(launch_digit_counts(L.d_keys, n, kb, passes, 8, 0, 8, is_float, L.counts, stream));
-  PA_CUDA(mark());
-  PA_CUDA(launch_scan_digits(L.counts, passes, 8, n, is_float, true, L.bin_start, L.ctrl, stream));
-  PA_CUDA(mark());
-  for (int p = 0; p < passes; ++p) {
-    OnesweepArgs a{};
-    a.keys_a = L.d_keys;
-    a.keys_b = L.d_tmp;
-    a.vals_a = L.d_vals;
-    a.vals_b = L.d_tvals;
-    a.n = n;
-    a.shift = 8u * (uint32_t)p;
-    a.pass = p;
-    a.is_float = is_float ? 1 : 0;
-    a.bin_start = L.bin_start + (size_t)p * 256;
-    a.status = L.status + (size_t)p * tiles * 256 * sb;
-    a.tile_counter = L.tile_ctr + p;
-    a.ctrl = L.ctrl;
-    a.err = ws->err;
-    PA_CUDA(launch_onesweep_pass(a, kb, has_vals, stream));
-    PA_CUDA(mark());
-  }
-  PA_CUDA(launch_final_copy(L.d_keys, L.d_tmp, L.d_vals, L.d_tvals, n, kb, L.ctrl, stream));
-  PA_CUDA(mark());
-  if (!keys_dev) PA_CUDA(cudaMemcpyAsync(keys, L.d_keys, key_bytes_total, cudaMemcpyDeviceToHost, stream));
+  PA_CUDA(enqueue_sort(sc, d_keys, d_tmp, d_vals, d_tvals, n, kb, is_float, ws->err, stream, mark));
+  if (!keys_dev) PA_CUDA(cudaMemcpyAsync(keys, d_keys, key_bytes_total, cudaMemcpyDeviceToHost, stream));
   if (has_vals && !vals_dev)
-    PA_CUDA(cudaMemcpyAsync(vals, L.d_vals, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    PA_CUDA(cudaMemcpyAsync(vals, d_vals, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
   const bool all_dev = keys_dev && (!has_vals || vals_dev);
   int rc = finish(ws, stream, !timed && opts && opts->async_device && all_dev);
   if (rc == PA_OK && timed) {
@@ -384,6 +343,63 @@ int sum_impl(const void* a, size_t n, int kb, uint64_t* out, const pa_opts* opts
 }
 
 }  // namespace
+
+size_t sort_scratch_bytes(size_t n, int kb, bool has_vals) {
+  SortScratch s{};
+  return sort_scratch_layout(nullptr, n, kb, has_vals, &s);
+}
+
+size_t sort_scratch_layout(char* base, size_t n, int kb, bool has_vals, SortScratch* s) {
+  const int passes = kb;  // 8-bit digits: one pass per key byte
+  const size_t tiles = ceil_div(n, onesweep_tile_keys(kb, has_vals));
+  const size_t sb = onesweep_status_bytes(n);
+  Carve c{base};
+  s->counts = c.take<unsigned long long>((size_t)passes * 256);
+  s->zero_begin = reinterpret_cast<char*>(s->counts);
+  s->tile_ctr = c.take<uint32_t>(passes);
+  s->status = c.take<char>((size_t)passes * tiles * 256 * sb);
+  s->zero_bytes = (size_t)(base + c.off - s->zero_begin);
+  s->bin_start = c.take<unsigned long long>((size_t)passes * 256);
+  s->ctrl = c.take<SortCtrl>(1);
+  s->tiles = tiles;
+  s->status_bytes = sb;
+  return c.off;
+}
+
+cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32_t* d_vals, uint32_t* d_tvals,
+                         size_t n, int kb, bool is_float, uint32_t* err, cudaStream_t stream,
+                         const std::function<cudaError_t()>& mark) {
+  const int passes = kb;
+  const bool has_vals = d_vals != nullptr;
+  auto m = [&]() { return mark ? mark() : cudaSuccess; };
+  cudaError_t e = cudaMemsetAsync(s.zero_begin, 0, s.zero_bytes, stream);
+  if (e == cudaSuccess) e = m();
+  if (e == cudaSuccess) e = launch_digit_counts(d_keys, n, kb, passes, 8, 0, 8, is_float, s.counts, stream);
+  if (e == cudaSuccess) e = m();
+  if (e == cudaSuccess) e = launch_scan_digits(s.counts, passes, 8, n, is_float, true, s.bin_start, s.ctrl, stream);
+  if (e == cudaSuccess) e = m();
+  for (int p = 0; p < passes && e == cudaSuccess; ++p) {
+    OnesweepArgs a{};
+    a.keys_a = d_keys;
+    a.keys_b = d_tmp;
+    a.vals_a = d_vals;
+    a.vals_b = d_tvals;
+    a.n = n;
+    a.shift = 8u * (uint32_t)p;
+    a.pass = p;
+    a.is_float = is_float ? 1 : 0;
+    a.bin_start = s.bin_start + (size_t)p * 256;
+    a.status = s.status + (size_t)p * s.tiles * 256 * s.status_bytes;
+    a.tile_counter = s.tile_ctr + p;
+    a.ctrl = s.ctrl;
+    a.err = err;
+    e = launch_onesweep_pass(a, kb, has_vals, stream);
+    if (e == cudaSuccess) e = m();
+  }
+  if (e == cudaSuccess) e = launch_final_copy(d_keys, d_tmp, d_vals, d_tvals, n, kb, s.ctrl, stream);
+  if (e == cudaSuccess) e = m();
+  return e;
+}
 
 int record_error(int status, const char* message) { return set_error(status, "%s", message); }
 
@@ -511,6 +527,11 @@ int pa_hist_byte_components_u32(const uint32_t* a, size_t n, uint64_t* out, cons
 int pa_hist_one_byte_u32(const uint32_t* a, size_t n, unsigned shift, uint64_t* out, const pa_opts* opts) {
   if (shift >= 32) return set_error(PA_ERR_ARG, "shift %u is not below 32", shift);
   return hist_impl(a, n, 4, 1, shift, 0, out, opts);
+}
+
+int pa_hist_one_byte_u64(const uint64_t* a, size_t n, unsigned shift, uint64_t* out, const pa_opts* opts) {
+  if (shift >= 64) return set_error(PA_ERR_ARG, "shift %u is not below 64", shift);
+  return hist_impl(a, n, 8, 1, shift, 0, out, opts);
 }
 
 int pa_hist_u8(const uint8_t* a, size_t n, uint64_t* out, const pa_opts* opts) {

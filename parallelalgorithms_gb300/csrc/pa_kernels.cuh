@@ -6,6 +6,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <cuda_runtime.h>
 
 namespace pa {
@@ -95,6 +96,29 @@ cudaError_t launch_onesweep_pass(const OnesweepArgs& a, int key_bytes, bool has_
 // left it in the scratch buffers (device-side decision from SortCtrl).
 cudaError_t launch_final_copy(void* keys_a, const void* keys_b, uint32_t* vals_a, const uint32_t* vals_b,
                               size_t n, int key_bytes, const SortCtrl* ctrl, cudaStream_t stream);
+
+// ---- whole sorts on device buffers (pa_capi.cu) ---------------------------
+// Per-call scratch of a device-resident sort: digit counts, tile tickets and
+// look-back words (zeroed by enqueue_sort), bin starts, pass control.
+struct SortScratch {
+  unsigned long long* counts;
+  uint32_t* tile_ctr;
+  char* status;
+  unsigned long long* bin_start;
+  SortCtrl* ctrl;
+  char* zero_begin;
+  size_t zero_bytes;
+  size_t tiles;
+  size_t status_bytes;
+};
+size_t sort_scratch_bytes(size_t n, int key_bytes, bool has_vals);
+// Carves the scratch from `base` (nullptr measures); returns its size.
+size_t sort_scratch_layout(char* base, size_t n, int key_bytes, bool has_vals, SortScratch* s);
+// Enqueues the whole sort (memset, histogram, scan, passes, final copy) of
+// device buffers on `stream`; `mark`, when set, runs between launches.
+cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32_t* d_vals, uint32_t* d_tvals,
+                         size_t n, int key_bytes, bool is_float, uint32_t* err, cudaStream_t stream,
+                         const std::function<cudaError_t()>& mark = {});
 
 // ---- sum (pa_sum.cu) -------------------------------------------------------
 // out = sum of keys[0, n) modulo 2^64.  partials holds sum_partials_needed()

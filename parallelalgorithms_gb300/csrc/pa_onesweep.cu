@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
   job.status = static_cast<S*>(args.status);
   job.err = args.err;
   uint32_t parity = 0;
-  onesweep_tile<K, HAS_VALS, BLOCK, ITEMS, S>(job, smem, parity);
+  onesweep_tile<K, HAS_VALS, BLOCK, ITEMS, S>(job, smem, s_bar, parity);
 }
 
 template <typename K>

@@ -206,11 +206,12 @@ struct TileJob {
 };
 
 // One tile of an onesweep digit pass (steps 2-6 above).  Called by all
-// BLOCK threads after a barrier that ends every earlier use of `smem`; the
-// mbarrier at G::kBarOff is initialised and `parity` is the phase the next
-// bulk copy completes (flipped here when one is used).
+// BLOCK threads after a barrier that ends every earlier use of `smem`;
+// `s_bar` is an initialised mbarrier outside the tile's layout and `parity`
+// the phase the next bulk copy completes (flipped here when one is used).
 template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, typename S>
-__device__ __forceinline__ void onesweep_tile(const TileJob<K, S>& job, unsigned char* smem, uint32_t& parity) {
+__device__ __forceinline__ void onesweep_tile(const TileJob<K, S>& job, unsigned char* smem, uint64_t* s_bar,
+                                              uint32_t& parity) {
   using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
   using SW = StatusWord<S>;
   constexpr int TILE = G::kTile;
@@ -221,7 +222,6 @@ __device__ __forceinline__ void onesweep_tile(const TileJob<K, S>& job, unsigned
   uint32_t* s_bin_start = reinterpret_cast<uint32_t*>(smem + G::kBinStartOff);
   uint32_t* s_bin_end = reinterpret_cast<uint32_t*>(smem + G::kBinEndOff);
   uint32_t* s_warp = reinterpret_cast<uint32_t*>(smem + G::kWarpTotOff);
-  uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + G::kBarOff);
   uint32_t* s_abort = reinterpret_cast<uint32_t*>(smem + G::kAbortOff);
 
   // No __restrict__/read-only path: in a batched launch the input of a pass

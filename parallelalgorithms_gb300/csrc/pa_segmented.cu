@@ -35,51 +35,12 @@
 #include "pa_gpu.h"
 #include "pa_kernels.cuh"
 #include "pa_onesweep_tile.cuh"
+#include "pa_segmented.cuh"
 
 namespace pa {
 namespace seg {
 
 using namespace os;
-
-constexpr int kBlock = 512;
-constexpr int kPasses = 4;                  // uint32 keys, 8-bit digits
-constexpr uint32_t kHistChunk = 64 * 1024;  // keys per HIST item
-constexpr int kHistLanes = 8;               // lane-banked copies of each counter
-constexpr uint32_t kMaxSegmentKeys = (1u << 30) - 1;  // 32-bit look-back words
-
-enum : uint32_t { ITEM_SMALL = 0, ITEM_HIST = 1, ITEM_SCAN = 2, ITEM_PASS = 3 };
-enum : uint32_t { ST_HIST = 0, ST_SCAN = 1, ST_PASS0 = 2, kStages = 2 + kPasses };
-
-struct Item {
-  uint32_t kind;
-  uint32_t pass;
-  uint32_t seg;  // segment index (SMALL) or large-segment index
-  uint32_t idx;  // tile (PASS) or chunk (HIST)
-};
-
-struct LargeSeg {
-  unsigned long long base;
-  uint32_t len;
-  uint32_t tiles;
-  uint32_t hist_chunks;
-  uint32_t tile_base;  // first tile of this segment in each pass's status array
-};
-
-struct PlanDev {
-  uint32_t* keys;
-  uint32_t* tmp;
-  const Item* items;
-  uint32_t num_items;
-  uint32_t total_tiles;
-  const unsigned long long* seg_off;
-  const LargeSeg* large;
-  uint32_t* head;                  // zeroed per run
-  uint32_t* done;                  // [large][kStages], zeroed per run
-  uint32_t* hist;                  // [large][4][256], zeroed per run
-  uint32_t* status;                // [kPasses][total_tiles][256], zeroed per run
-  unsigned long long* bin_start;   // [large][4][256]
-  uint32_t* err;
-};
 
 // Bounded wait until *ctr >= need (acquire).  Thread 0 only.
 __device__ __forceinline__ void wait_count(const uint32_t* ctr, uint32_t need, uint32_t* err) {
@@ -126,7 +87,8 @@ __device__ __forceinline__ void scan_item(const PlanDev& P, const Item& it, unsi
 }
 
 template <int PASS_ITEMS>
-__device__ __forceinline__ void pass_item(const PlanDev& P, const Item& it, unsigned char* smem, uint32_t& parity) {
+__device__ __forceinline__ void pass_item(const PlanDev& P, const Item& it, unsigned char* smem, uint64_t* bar,
+                                          uint32_t& parity) {
   const LargeSeg L = P.large[it.seg];
   const bool even = (it.pass & 1u) == 0;
   TileJob<uint32_t, uint32_t> job;
@@ -142,7 +104,7 @@ __device__ __forceinline__ void pass_item(const PlanDev& P, const Item& it, unsi
   job.bin_start = P.bin_start + (size_t)it.seg * 1024 + it.pass * 256;
   job.status = P.status + ((size_t)it.pass * P.total_tiles + L.tile_base) * 256;
   job.err = P.err;
-  onesweep_tile<uint32_t, false, kBlock, PASS_ITEMS, uint32_t>(job, smem, parity);
+  onesweep_tile<uint32_t, false, kBlock, PASS_ITEMS, uint32_t>(job, smem, bar, parity);
 }
 
 template <int SMALL_ITEMS>
@@ -169,11 +131,13 @@ __device__ __forceinline__ void small_item(const PlanDev& P, const Item& it, uns
 
 template <int PASS_ITEMS, int SMALL_ITEMS>
 __global__ void __launch_bounds__(kBlock, 2) segsort_kernel(const PlanDev P) {
-  using GP = Geometry<uint32_t, false, kBlock, PASS_ITEMS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ Item s_item;
   __shared__ uint32_t s_index;
-  uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + GP::kBarOff);
+  // The bulk-copy barrier lives outside the dynamic area, which every item
+  // kind lays out differently.
+  __shared__ __align__(8) uint64_t s_bar_storage;
+  uint64_t* s_bar = &s_bar_storage;
   if (threadIdx.x == 0) {
     mbar_init(s_bar, 1);
     mbar_fence_init();
@@ -209,7 +173,7 @@ __global__ void __launch_bounds__(kBlock, 2) segsort_kernel(const PlanDev P) {
     else if (it.kind == ITEM_SCAN)
       scan_item(P, it, smem);
     else
-      pass_item<PASS_ITEMS>(P, it, smem, parity);
+      pass_item<PASS_ITEMS>(P, it, smem, s_bar, parity);
     __syncthreads();
     if (it.kind != ITEM_SMALL && threadIdx.x == 0) {
       __threadfence();
@@ -220,8 +184,6 @@ __global__ void __launch_bounds__(kBlock, 2) segsort_kernel(const PlanDev P) {
 }
 
 // ---- host side ---------------------------------------------------------------
-using KernelFn = void (*)(const PlanDev);
-
 template <int PI, int SI>
 constexpr size_t smem_bytes_for() {
   using GP = Geometry<uint32_t, false, kBlock, PI>;
@@ -232,12 +194,6 @@ constexpr size_t smem_bytes_for() {
   return b;
 }
 
-struct KernelChoice {
-  KernelFn fn;
-  size_t smem;
-  uint32_t pass_tile;
-  uint32_t small_tile;
-};
 
 template <int PI, int SI>
 KernelChoice choice() {
@@ -257,6 +213,152 @@ bool pick_kernel(int tile_keys, int small_cutoff, KernelChoice* out) {
   return true;
 }
 
+// ---- host-side planning --------------------------------------------------------
+int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segsort_config* cfg, HostPlan* hp) {
+  pa_segsort_config c{};
+  if (cfg) c = *cfg;
+  for (int r : c.reserved)
+    if (r) return record_error(PA_ERR_ARG, "pa_segsort_config.reserved must be zero");
+  if (c.small_cutoff == 0) c.small_cutoff = 4096;
+  if (c.tile_keys == 0) c.tile_keys = 8192;
+  if (c.digit_bits == 0) c.digit_bits = 8;
+  if (c.digit_bits != 8) return record_error(PA_ERR_ARG, "digit_bits must be 8 for the batched sort");
+  KernelChoice kc{};
+  if (!pick_kernel(c.tile_keys, c.small_cutoff, &kc))
+    return record_error(PA_ERR_ARG, "tile_keys must be 4096 or 8192 and small_cutoff 2048, 4096 or 8192");
+  const uint64_t* off = off_host;
+  for (size_t i = 0; i < num_segments; ++i) {
+    if (off[i + 1] < off[i]) return record_error(PA_ERR_ARG, "seg_offsets must be non-decreasing");
+    if (off[i + 1] - off[i] > kMaxSegmentKeys)
+      return record_error(PA_ERR_ARG, "a segment exceeds 2^30 - 1 keys (the batched sort's limit)");
+  }
+  hp->cfg = c;
+  hp->kc = kc;
+  hp->off.assign(off, off + num_segments + 1);
+  hp->items.clear();
+  hp->large.clear();
+  std::vector<uint32_t> small_ids;
+  uint32_t total_tiles = 0;
+  for (size_t i = 0; i < num_segments; ++i) {
+    const uint64_t len = off[i + 1] - off[i];
+    if (len <= 1) continue;
+    if (len <= (uint64_t)kc.small_tile && len <= (uint64_t)c.small_cutoff) {
+      small_ids.push_back((uint32_t)i);
+    } else {
+      LargeSeg L{};
+      L.base = off[i];
+      L.len = (uint32_t)len;
+      L.tiles = (uint32_t)((len + kc.pass_tile - 1) / kc.pass_tile);
+      L.hist_chunks = (uint32_t)((len + kHistChunk - 1) / kHistChunk);
+      L.tile_base = total_tiles;
+      total_tiles += L.tiles;
+      hp->large.push_back(L);
+    }
+  }
+  // largest small segments first (they take longest)
+  std::stable_sort(small_ids.begin(), small_ids.end(),
+                   [&](uint32_t a, uint32_t b) { return off[a + 1] - off[a] > off[b + 1] - off[b]; });
+  auto& items = hp->items;
+  size_t next_small = 0;
+  const size_t gaps = 1 + 1 + kPasses;  // after HIST, SCAN, and each pass but the last
+  auto add_small = [&](size_t share_of) {
+    const size_t upto = std::min(small_ids.size(), (small_ids.size() * share_of + gaps - 1) / gaps);
+    for (; next_small < upto; ++next_small) items.push_back({ITEM_SMALL, 0, small_ids[next_small], 0});
+  };
+  const uint32_t nlarge = (uint32_t)hp->large.size();
+  for (uint32_t l = 0; l < nlarge; ++l)
+    for (uint32_t ch = 0; ch < hp->large[l].hist_chunks; ++ch) items.push_back({ITEM_HIST, 0, l, ch});
+  add_small(1);
+  for (uint32_t l = 0; l < nlarge; ++l) items.push_back({ITEM_SCAN, 0, l, 0});
+  add_small(2);
+  for (uint32_t p = 0; p < (uint32_t)kPasses; ++p) {
+    for (uint32_t l = 0; l < nlarge; ++l)
+      for (uint32_t t = 0; t < hp->large[l].tiles; ++t) items.push_back({ITEM_PASS, p, l, t});
+    add_small(3 + p);
+  }
+  add_small(gaps);
+  hp->total_tiles = total_tiles;
+  hp->num_small = (uint32_t)small_ids.size();
+  hp->num_large = nlarge;
+  // device layout
+  const size_t nl = std::max<size_t>(nlarge, 1);
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    o = (o + 255) & ~(size_t)255;
+    const size_t at = o;
+    o += bytes;
+    return at;
+  };
+  hp->o_items = take(std::max<size_t>(items.size(), 1) * sizeof(Item));
+  hp->o_off = take(hp->off.size() * 8);
+  hp->o_large = take(nl * sizeof(LargeSeg));
+  hp->o_bins = take(nl * 1024 * 8);
+  hp->o_err = take(256);
+  hp->o_head = take(256);
+  hp->o_done = take(nl * kStages * 4);
+  hp->o_hist = take(nl * 1024 * 4);
+  hp->o_status = take((size_t)kPasses * std::max<uint32_t>(total_tiles, 1) * 256 * 4);
+  hp->bytes = o;
+  return PA_OK;
+}
+
+PlanDev device_view(const HostPlan& hp, char* dev, uint32_t* keys, uint32_t* tmp) {
+  PlanDev d{};
+  d.keys = keys;
+  d.tmp = tmp;
+  d.items = reinterpret_cast<const Item*>(dev + hp.o_items);
+  d.num_items = (uint32_t)hp.items.size();
+  d.total_tiles = hp.total_tiles;
+  d.seg_off = reinterpret_cast<const unsigned long long*>(dev + hp.o_off);
+  d.large = reinterpret_cast<const LargeSeg*>(dev + hp.o_large);
+  d.head = reinterpret_cast<uint32_t*>(dev + hp.o_head);
+  d.done = reinterpret_cast<uint32_t*>(dev + hp.o_done);
+  d.hist = reinterpret_cast<uint32_t*>(dev + hp.o_hist);
+  d.status = reinterpret_cast<uint32_t*>(dev + hp.o_status);
+  d.bin_start = reinterpret_cast<unsigned long long*>(dev + hp.o_bins);
+  d.err = reinterpret_cast<uint32_t*>(dev + hp.o_err);
+  return d;
+}
+
+cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  if (!hp.items.empty())
+    e = cudaMemcpyAsync(dev + hp.o_items, hp.items.data(), hp.items.size() * sizeof(Item), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dev + hp.o_off, hp.off.data(), hp.off.size() * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && !hp.large.empty())
+    e = cudaMemcpyAsync(dev + hp.o_large, hp.large.data(), hp.large.size() * sizeof(LargeSeg),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dev + hp.o_err, 0, 256, s);
+  return e;
+}
+
+unsigned plan_grid(const HostPlan& hp) {
+  static bool configured[2][3] = {};
+  const int pi = hp.kc.pass_tile == 4096 ? 0 : 1;
+  const int si = hp.kc.small_tile == 2048 ? 0 : hp.kc.small_tile == 4096 ? 1 : 2;
+  if (!configured[pi][si]) {
+    cudaFuncSetAttribute(hp.kc.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hp.kc.smem);
+    configured[pi][si] = true;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hp.kc.fn, kBlock, hp.kc.smem) != cudaSuccess) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)device_info().sm_count;
+  const uint32_t items = (uint32_t)hp.items.size();
+  if (items < grid) grid = std::max<uint32_t>(items, 1);
+  return grid;
+}
+
+cudaError_t launch_plan(const HostPlan& hp, const PlanDev& pd, char* dev, unsigned grid, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(dev + hp.o_head, 0, hp.bytes - hp.o_head, s);
+  if (e != cudaSuccess || hp.items.empty()) return e;
+  hp.kc.fn<<<grid, kBlock, hp.kc.smem, s>>>(pd);
+  return cudaGetLastError();
+}
+
 }  // namespace seg
 }  // namespace pa
 
@@ -267,13 +369,10 @@ struct pa_segsort_plan {
   int device = -1;
   size_t num_segments = 0;
   unsigned long long total_keys = 0;
-  pa_segsort_config cfg{};
-  KernelChoice kc{};
+  HostPlan hp;
   unsigned grid = 0;
   char* dev = nullptr;
-  size_t zero_off = 0, zero_bytes = 0;
   PlanDev pd{};
-  uint32_t num_items = 0, num_small = 0, num_large = 0;
   uint32_t* err_host = nullptr;
   cudaStream_t cap_stream = nullptr;
   cudaGraph_t graph = nullptr;
@@ -317,11 +416,7 @@ void destroy_graph(pa_segsort_plan* p) {
 }
 
 int enqueue(pa_segsort_plan* p, cudaStream_t s) {
-  PA_SEG_CUDA(cudaMemsetAsync(p->dev + p->zero_off, 0, p->zero_bytes, s));
-  if (p->num_items) {
-    p->kc.fn<<<p->grid, kBlock, p->kc.smem, s>>>(p->pd);
-    PA_SEG_CUDA(cudaGetLastError());
-  }
+  PA_SEG_CUDA(launch_plan(p->hp, p->pd, p->dev, p->grid, s));
   return PA_OK;
 }
 
@@ -334,17 +429,6 @@ int pa_segsort_plan_create(const uint64_t* seg_offsets, size_t num_segments, con
   if (!out) return record_error(PA_ERR_ARG, "out is NULL");
   *out = nullptr;
   if (!seg_offsets) return record_error(PA_ERR_ARG, "seg_offsets is NULL");
-  pa_segsort_config c{};
-  if (cfg) c = *cfg;
-  for (int r : c.reserved)
-    if (r) return record_error(PA_ERR_ARG, "pa_segsort_config.reserved must be zero");
-  if (c.small_cutoff == 0) c.small_cutoff = 4096;
-  if (c.tile_keys == 0) c.tile_keys = 8192;
-  if (c.digit_bits == 0) c.digit_bits = 8;
-  if (c.digit_bits != 8) return record_error(PA_ERR_ARG, "digit_bits must be 8 for the batched sort");
-  KernelChoice kc{};
-  if (!pick_kernel(c.tile_keys, c.small_cutoff, &kc))
-    return record_error(PA_ERR_ARG, "tile_keys must be 4096 or 8192 and small_cutoff 2048, 4096 or 8192");
   int count = 0;
   if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
     cudaGetLastError();
@@ -357,129 +441,38 @@ int pa_segsort_plan_create(const uint64_t* seg_offsets, size_t num_segments, con
   } else {
     std::memcpy(off.data(), seg_offsets, off.size() * 8);
   }
-  for (size_t i = 0; i < num_segments; ++i) {
-    if (off[i + 1] < off[i]) return record_error(PA_ERR_ARG, "seg_offsets must be non-decreasing");
-    if (off[i + 1] - off[i] > kMaxSegmentKeys)
-      return record_error(PA_ERR_ARG, "a segment exceeds 2^30 - 1 keys (the batched sort's limit)");
-  }
-
-  // ---- classify segments and build the queue ----------------------------------
-  std::vector<uint32_t> small_ids;
-  std::vector<LargeSeg> large;
-  std::vector<uint32_t> large_seg_id;
-  uint32_t total_tiles = 0;
-  for (size_t i = 0; i < num_segments; ++i) {
-    const uint64_t len = off[i + 1] - off[i];
-    if (len <= 1) continue;
-    if (len <= (uint64_t)kc.small_tile && len <= (uint64_t)c.small_cutoff) {
-      small_ids.push_back((uint32_t)i);
-    } else {
-      LargeSeg L{};
-      L.base = off[i];
-      L.len = (uint32_t)len;
-      L.tiles = (uint32_t)((len + kc.pass_tile - 1) / kc.pass_tile);
-      L.hist_chunks = (uint32_t)((len + kHistChunk - 1) / kHistChunk);
-      L.tile_base = total_tiles;
-      total_tiles += L.tiles;
-      large.push_back(L);
-      large_seg_id.push_back((uint32_t)i);
-    }
-  }
-  // largest small segments first (they take longest)
-  std::stable_sort(small_ids.begin(), small_ids.end(),
-                   [&](uint32_t a, uint32_t b) { return off[a + 1] - off[a] > off[b + 1] - off[b]; });
-  std::vector<Item> items;
-  size_t next_small = 0;
-  const size_t gaps = 1 + 1 + kPasses;  // after HIST, SCAN, and each pass but the last
-  auto add_small = [&](size_t share_of) {
-    const size_t upto = std::min(small_ids.size(), (small_ids.size() * share_of + gaps - 1) / gaps);
-    for (; next_small < upto; ++next_small) items.push_back({ITEM_SMALL, 0, small_ids[next_small], 0});
-  };
-  for (uint32_t l = 0; l < large.size(); ++l)
-    for (uint32_t ch = 0; ch < large[l].hist_chunks; ++ch) items.push_back({ITEM_HIST, 0, l, ch});
-  add_small(1);
-  for (uint32_t l = 0; l < large.size(); ++l) items.push_back({ITEM_SCAN, 0, l, 0});
-  add_small(2);
-  for (uint32_t p = 0; p < (uint32_t)kPasses; ++p) {
-    for (uint32_t l = 0; l < large.size(); ++l)
-      for (uint32_t t = 0; t < large[l].tiles; ++t) items.push_back({ITEM_PASS, p, l, t});
-    add_small(3 + p);
-  }
-  add_small(gaps);
-
-  // ---- device memory ------------------------------------------------------------
   auto* p = new pa_segsort_plan();
+  if (int rc = build_host_plan(off.data(), num_segments, cfg, &p->hp)) {
+    delete p;
+    return rc;
+  }
   cudaGetDevice(&p->device);
   p->num_segments = num_segments;
   p->total_keys = num_segments ? off[num_segments] : 0;
-  p->cfg = c;
-  p->kc = kc;
-  p->num_items = (uint32_t)items.size();
-  p->num_small = (uint32_t)small_ids.size();
-  p->num_large = (uint32_t)large.size();
-  const size_t nl = std::max<size_t>(large.size(), 1);
-  size_t o = 0;
-  auto take = [&](size_t bytes) {
-    o = (o + 255) & ~(size_t)255;
-    const size_t at = o;
-    o += bytes;
-    return at;
-  };
-  const size_t o_items = take(std::max<size_t>(items.size(), 1) * sizeof(Item));
-  const size_t o_off = take(off.size() * 8);
-  const size_t o_large = take(nl * sizeof(LargeSeg));
-  const size_t o_bins = take(nl * 1024 * 8);
-  const size_t o_err = take(256);
-  const size_t o_head = take(256);
-  const size_t o_done = take(nl * kStages * 4);
-  const size_t o_hist = take(nl * 1024 * 4);
-  const size_t o_status = take((size_t)kPasses * std::max<uint32_t>(total_tiles, 1) * 256 * 4);
-  const size_t total = o;
-  cudaError_t e = cudaMalloc(&p->dev, total);
+  cudaError_t e = cudaMalloc(&p->dev, p->hp.bytes);
   if (e != cudaSuccess) {
     delete p;
     return cfail(e, "cudaMalloc(plan)");
   }
   e = cudaMallocHost(&p->err_host, sizeof(uint32_t));
-  if (e == cudaSuccess && !items.empty())
-    e = cudaMemcpy(p->dev + o_items, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(p->dev + o_off, off.data(), off.size() * 8, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && !large.empty())
-    e = cudaMemcpy(p->dev + o_large, large.data(), large.size() * sizeof(LargeSeg), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemset(p->dev + o_err, 0, 256);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(kc.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kc.smem);
-  int per_sm = 0;
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kc.fn, kBlock, kc.smem);
+  if (e == cudaSuccess) e = upload_plan(p->hp, p->dev, (cudaStream_t)0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)0);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     pa_segsort_plan_destroy(p);
     return cfail(e, "plan set-up");
   }
-  p->grid = (unsigned)std::max(1, per_sm) * (unsigned)device_info().sm_count;
-  if (p->num_items < p->grid) p->grid = std::max<uint32_t>(p->num_items, 1);
-  p->zero_off = o_head;
-  p->zero_bytes = total - o_head;
-  PlanDev& d = p->pd;
-  d.items = reinterpret_cast<const Item*>(p->dev + o_items);
-  d.num_items = p->num_items;
-  d.total_tiles = total_tiles;
-  d.seg_off = reinterpret_cast<const unsigned long long*>(p->dev + o_off);
-  d.large = reinterpret_cast<const LargeSeg*>(p->dev + o_large);
-  d.head = reinterpret_cast<uint32_t*>(p->dev + o_head);
-  d.done = reinterpret_cast<uint32_t*>(p->dev + o_done);
-  d.hist = reinterpret_cast<uint32_t*>(p->dev + o_hist);
-  d.status = reinterpret_cast<uint32_t*>(p->dev + o_status);
-  d.bin_start = reinterpret_cast<unsigned long long*>(p->dev + o_bins);
-  d.err = reinterpret_cast<uint32_t*>(p->dev + o_err);
+  p->grid = plan_grid(p->hp);
+  p->pd = device_view(p->hp, p->dev, nullptr, nullptr);
   *out = p;
   return PA_OK;
 }
 
 int pa_segsort_plan_info(const pa_segsort_plan* p, uint32_t* num_small, uint32_t* num_large, uint32_t* num_items) {
   if (!p) return record_error(PA_ERR_ARG, "plan is NULL");
-  if (num_small) *num_small = p->num_small;
-  if (num_large) *num_large = p->num_large;
-  if (num_items) *num_items = p->num_items;
+  if (num_small) *num_small = p->hp.num_small;
+  if (num_large) *num_large = p->hp.num_large;
+  if (num_items) *num_items = (uint32_t)p->hp.items.size();
   return PA_OK;
 }
 
@@ -491,7 +484,7 @@ int pa_segsort_plan_run(pa_segsort_plan* p, uint32_t* keys, uint32_t* tmp, const
   cudaStream_t s = opts ? static_cast<cudaStream_t>(opts->stream) : (cudaStream_t)0;
   p->pd.keys = keys;
   p->pd.tmp = tmp;
-  if (p->cfg.use_graph) {
+  if (p->hp.cfg.use_graph) {
     if (!p->exec || p->g_keys != keys || p->g_tmp != tmp) {
       destroy_graph(p);
       PA_SEG_CUDA(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));

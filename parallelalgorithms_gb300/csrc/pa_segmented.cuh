@@ -1,0 +1,92 @@
+// Host-side interface of the batched segmented sort (pa_segmented.cu), used
+// by its C ABI and by the serving loop (pa_serve.cu) to launch coalesced
+// batches on their own streams with caller-provided device memory.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "pa_gpu.h"
+
+namespace pa {
+namespace seg {
+
+constexpr int kBlock = 512;
+constexpr int kPasses = 4;                  // uint32 keys, 8-bit digits
+constexpr uint32_t kHistChunk = 64 * 1024;  // keys per HIST item
+constexpr int kHistLanes = 8;               // lane-banked copies of each counter
+constexpr uint32_t kMaxSegmentKeys = (1u << 30) - 1;  // 32-bit look-back words
+
+enum : uint32_t { ITEM_SMALL = 0, ITEM_HIST = 1, ITEM_SCAN = 2, ITEM_PASS = 3 };
+enum : uint32_t { ST_HIST = 0, ST_SCAN = 1, ST_PASS0 = 2, kStages = 2 + kPasses };
+
+struct Item {
+  uint32_t kind;
+  uint32_t pass;
+  uint32_t seg;  // segment index (SMALL) or large-segment index
+  uint32_t idx;  // tile (PASS) or chunk (HIST)
+};
+
+struct LargeSeg {
+  unsigned long long base;
+  uint32_t len;
+  uint32_t tiles;
+  uint32_t hist_chunks;
+  uint32_t tile_base;  // first tile of this segment in each pass's status array
+};
+
+struct PlanDev {
+  uint32_t* keys;
+  uint32_t* tmp;
+  const Item* items;
+  uint32_t num_items;
+  uint32_t total_tiles;
+  const unsigned long long* seg_off;
+  const LargeSeg* large;
+  uint32_t* head;                  // zeroed per run
+  uint32_t* done;                  // [large][kStages], zeroed per run
+  uint32_t* hist;                  // [large][4][256], zeroed per run
+  uint32_t* status;                // [kPasses][total_tiles][256], zeroed per run
+  unsigned long long* bin_start;   // [large][4][256]
+  uint32_t* err;
+};
+
+using KernelFn = void (*)(const PlanDev);
+
+// The persistent kernel instantiation for a (tile, small cutoff) choice.
+struct KernelChoice {
+  KernelFn fn;
+  size_t smem;
+  uint32_t pass_tile;
+  uint32_t small_tile;
+};
+
+// A batch planned on the host: the work queue, the large segments, the
+// offsets, and the layout of the device block the launch needs.
+struct HostPlan {
+  pa_segsort_config cfg{};
+  KernelChoice kc{};
+  std::vector<Item> items;
+  std::vector<LargeSeg> large;
+  std::vector<uint64_t> off;
+  uint32_t total_tiles = 0, num_small = 0, num_large = 0;
+  size_t o_items = 0, o_off = 0, o_large = 0, o_bins = 0, o_err = 0, o_head = 0, o_done = 0, o_hist = 0,
+         o_status = 0, bytes = 0;
+};
+
+// Validates the offsets and plans the queue and the device block layout.
+int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segsort_config* cfg, HostPlan* hp);
+// Pointers of a device block laid out by `hp` (keys / tmp: the batch's keys).
+PlanDev device_view(const HostPlan& hp, char* dev, uint32_t* keys, uint32_t* tmp);
+// Copies the queue, offsets and segment table into the block; clears its error word.
+cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s);
+// Persistent grid for the plan's kernel on the current device.
+unsigned plan_grid(const HostPlan& hp);
+// Clears the per-run state and launches the persistent kernel.
+cudaError_t launch_plan(const HostPlan& hp, const PlanDev& pd, char* dev, unsigned grid, cudaStream_t s);
+
+}  // namespace seg
+}  // namespace pa
