@@ -447,6 +447,51 @@ def batched_extra(lib, _native, workloads, stream, peak) -> dict:
             "achieved_gbs": model_bytes / (ms / 1e3) / 1e9, "frac": model_bytes / (ms / 1e3) / 1e9 / peak}
 
 
+def serving_extra(count: int = 120) -> dict:
+    """C5: `count` requests (70 % sort, 20 % select at random k, 10 % 256-bin
+    histogram; sizes log-uniform in [1e4, 5e7]; uint32 / uint64 keys 50/50;
+    seed 1239), pinned host buffers, 64 GiB budget.  The plain per-request
+    form (one synchronous call after another) against the server at several
+    Poisson arrival rates; every served result is checked against the plain
+    one."""
+    from parallelalgorithms_gb300 import serving
+    specs = serving.make_specs(count)
+    bufs = serving.materialize(specs)
+    total = sum(s.n for s in specs)
+    serving.run_plain(specs[:8], bufs[:8])  # warm the plain path's workspace
+    per_call: list = []
+    plain_res, plain_s = serving.run_plain(specs, bufs, per_call)
+    plain_sorted = {i: b[0].copy() for i, (s, b) in enumerate(zip(specs, bufs)) if s.op == serving.REQ_SORT and
+                    i % 10 == 0}
+    lat = np.array(per_call) * 1e3
+    out = {"requests": count, "keys": int(total),
+           "mix": "70% sort / 20% select / 10% histogram, sizes log-uniform [1e4, 5e7], u32/u64 50/50, seed 1239",
+           "budget_bytes": 64 << 30,
+           "plain_per_request": {"keys_per_s": total / plain_s, "seconds": plain_s,
+                                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                                 "latency": "each call's own duration (no queueing)"}}
+    with serving.Server(budget_bytes=64 << 30) as srv:  # warm the server's memory pool
+        serving.run_served(srv, specs[:8], bufs[:8], None)
+        for rate in (None, 400.0, 200.0, 100.0):
+            reqs = serving.run_served(srv, specs, bufs, rate)
+            ok = all(r.c.status == 0 for r in reqs)
+            for i, (s, r, (buf, _, _)) in enumerate(zip(specs, reqs, bufs)):
+                if s.op == serving.REQ_SORT:
+                    ok = ok and bool(np.all(buf[1:] >= buf[:-1]))
+                    if i in plain_sorted:
+                        ok = ok and np.array_equal(buf, plain_sorted[i])
+                else:
+                    ok = ok and np.array_equal(r.result, plain_res[i])
+            span = max(r.c.t_done for r in reqs) - min(r.c.t_submit for r in reqs)
+            key = "saturating" if rate is None else f"poisson_{int(rate)}_per_s"
+            out[f"served_{key}"] = {"keys_per_s": total / span, "makespan_s": span,
+                                    "speedup_vs_plain_per_request": plain_s / span, "results_match_plain": ok,
+                                    **serving.latency_stats(reqs),
+                                    "latency": "submit to completion (includes queueing)"}
+        out["server_stats"] = srv.stats()
+    return out
+
+
 def run_extras(pa, lib, _native, workloads, n, stream, peak) -> dict:
     """Other 100M workloads of the same path, device-resident, median of 5."""
     import torch
@@ -514,6 +559,7 @@ def run_extras(pa, lib, _native, workloads, n, stream, peak) -> dict:
         _native.call("pa_stream_check", P(stream.cuda_stream))
         del d
     out["batched_segmented_sort_4096_arrays"] = batched_extra(lib, _native, workloads, stream, peak)
+    out["serving_c5"] = serving_extra()
     return out
 
 

@@ -159,7 +159,8 @@ def materialize(specs: list[Spec], pinned: bool = True):
 
 def run_served(server: Server, specs: list[Spec], bufs, rate: float | None, seed: int = 7) -> list[Request]:
     """Submits the requests with Poisson inter-arrival times (rate requests/s;
-    None = all at once) and waits for all of them."""
+    None = all at once) and waits for all of them.  The inputs are restored
+    before the first submission."""
     rng = np.random.default_rng(seed)
     reqs = []
     for s, (buf, _, src) in zip(specs, bufs):
@@ -176,14 +177,17 @@ def run_served(server: Server, specs: list[Spec], bufs, rate: float | None, seed
     return reqs
 
 
-def run_plain(specs: list[Spec], bufs) -> tuple[list, float]:
-    """One plain synchronous call per request (the per-request form).
-    Returns the results and the total wall time."""
+def run_plain(specs: list[Spec], bufs, per_call: list | None = None) -> tuple[list, float]:
+    """One plain synchronous call per request (the per-request form), one
+    after another.  Returns the results and the total wall time of the calls
+    (restoring each input before its call is not timed); per_call, if given,
+    receives each call's own duration."""
     results = []
-    t0 = time.perf_counter()
+    total = 0.0
     for s, (buf, _, src) in zip(specs, bufs):
         np.copyto(buf, src)
         kk = "u32" if s.key_kind == KEY_U32 else "u64"
+        t0 = time.perf_counter()
         if s.op == REQ_SORT:
             call(f"pa_sort_{kk}", P(buf.ctypes.data), None, s.n, None)
             results.append(None)
@@ -195,7 +199,11 @@ def run_plain(specs: list[Spec], bufs) -> tuple[list, float]:
             out = np.zeros(256, np.uint64)
             call(f"pa_hist_one_byte_{kk}", P(buf.ctypes.data), s.n, 0, P(out.ctypes.data), None)
             results.append(out)
-    return results, time.perf_counter() - t0
+        dt = time.perf_counter() - t0
+        total += dt
+        if per_call is not None:
+            per_call.append(dt)
+    return results, total
 
 
 def latency_stats(reqs: list[Request]) -> dict:
