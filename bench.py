@@ -470,8 +470,8 @@ def serving_extra(count: int = 120) -> dict:
            "plain_per_request": {"keys_per_s": total / plain_s, "seconds": plain_s,
                                  "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                                  "latency": "each call's own duration (no queueing)"}}
-    with serving.Server(budget_bytes=64 << 30) as srv:  # warm the server's memory pool
-        serving.run_served(srv, specs[:8], bufs[:8], None)
+    with serving.Server(budget_bytes=64 << 30, max_inflight=8, num_streams=8) as srv:
+        serving.run_served(srv, specs, bufs, None)  # warm the server's stream-ordered memory pool
         for rate in (None, 400.0, 200.0, 100.0):
             reqs = serving.run_served(srv, specs, bufs, rate)
             ok = all(r.c.status == 0 for r in reqs)

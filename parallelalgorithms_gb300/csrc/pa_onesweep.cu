@@ -31,6 +31,7 @@
 //      of a bin to consecutive addresses.
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 
 #include "pa_common.cuh"
 #include "pa_kernels.cuh"
@@ -41,7 +42,7 @@ namespace {
 
 using namespace os;
 
-template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S>
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S, bool MULTISPLIT>
 __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArgs args) {
   using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
   constexpr int TILE = G::kTile;
@@ -76,7 +77,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
   job.status = static_cast<S*>(args.status);
   job.err = args.err;
   uint32_t parity = 0;
-  onesweep_tile<K, HAS_VALS, BLOCK, ITEMS, S>(job, smem, s_bar, parity);
+  if constexpr (MULTISPLIT)
+    onesweep_tile_multisplit<K, HAS_VALS, BLOCK, ITEMS, S>(job, smem, s_bar, parity);
+  else
+    onesweep_tile<K, HAS_VALS, BLOCK, ITEMS, S>(job, smem, s_bar, parity);
 }
 
 template <typename K>
@@ -118,10 +122,21 @@ GeomChoice active_geometry() {
   return kGeomU64Kv[geometry_index(3)];
 }
 
-template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S>
-cudaError_t launch_g(const OnesweepArgs& a, cudaStream_t stream) {
+// Ranking method of the uint32 keys-only pass: the in-tile counting sort
+// (default) or the warp multisplit (PA_ONESWEEP_RANK=multisplit).
+bool use_multisplit() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("PA_ONESWEEP_RANK");
+    v = (e && std::strcmp(e, "multisplit") == 0) ? 1 : 0;
+  }
+  return v == 1;
+}
+
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S, bool MS>
+cudaError_t launch_g2(const OnesweepArgs& a, cudaStream_t stream) {
   using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
-  auto kern = onesweep_kernel<K, HAS_VALS, BLOCK, ITEMS, MINB, S>;
+  auto kern = onesweep_kernel<K, HAS_VALS, BLOCK, ITEMS, MINB, S, MS>;
   static bool configured = false;  // one attribute call per instantiation
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kBytes);
@@ -131,6 +146,14 @@ cudaError_t launch_g(const OnesweepArgs& a, cudaStream_t stream) {
   const size_t tiles = ceil_div(a.n, (size_t)G::kTile);
   kern<<<(unsigned)tiles, BLOCK, G::kBytes, stream>>>(a);
   return cudaGetLastError();
+}
+
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S>
+cudaError_t launch_g(const OnesweepArgs& a, cudaStream_t stream) {
+  if constexpr (sizeof(K) == 4 && !HAS_VALS) {
+    if (use_multisplit()) return launch_g2<K, HAS_VALS, BLOCK, ITEMS, MINB, S, true>(a, stream);
+  }
+  return launch_g2<K, HAS_VALS, BLOCK, ITEMS, MINB, S, false>(a, stream);
 }
 
 template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB>

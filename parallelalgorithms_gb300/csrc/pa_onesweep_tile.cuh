@@ -404,5 +404,253 @@ __device__ __forceinline__ void onesweep_tile(const TileJob<K, S>& job, unsigned
 }
 
 
+// 8-bit warp multisplit: the mask of lanes whose digit equals this lane's,
+// from eight ballots (no match instruction: on this GPU it runs on a slow
+// pipe).  For bit b: p = bit b of d; ballot(p); keep lanes that agree.
+__device__ __forceinline__ uint32_t match_digit8(uint32_t d) {
+  uint32_t peers = 0xFFFFFFFFu;
+#define PA_MATCH_BIT(B)                                         \
+  asm("{\n\t.reg .pred p;\n\t.reg .b32 t;\n\t"                   \
+      "and.b32 t, %1, " #B ";\n\t"                                \
+      "setp.ne.u32 p, t, 0;\n\t"                                  \
+      "vote.sync.ballot.b32 t, p, 0xffffffff;\n\t"                \
+      "@!p not.b32 t, t;\n\t"                                     \
+      "and.b32 %0, %0, t;\n\t}"                                   \
+      : "+r"(peers)                                              \
+      : "r"(d));
+  PA_MATCH_BIT(1)
+  PA_MATCH_BIT(2)
+  PA_MATCH_BIT(4)
+  PA_MATCH_BIT(8)
+  PA_MATCH_BIT(16)
+  PA_MATCH_BIT(32)
+  PA_MATCH_BIT(64)
+  PA_MATCH_BIT(128)
+#undef PA_MATCH_BIT
+  return peers;
+}
+
+// The same tile job as onesweep_tile, ranked by warp multisplit instead of
+// the in-tile counting sort: warp w owns the contiguous run
+// [w * 32 * ITEMS, (w + 1) * 32 * ITEMS) of the tile, lane l its items
+// j * 32 + l; for each item the lanes holding the same digit are found with
+// match_digit8, the lowest of them bumps the warp's counter for that digit
+// and every lane takes counter + peers below it, so ranks follow tile order.
+// Per-bin warp counters are scanned across warps into tile offsets; keys are
+// staged in shared memory at their in-tile sorted position and written out
+// as in onesweep_tile.
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, typename S>
+__device__ __forceinline__ void onesweep_tile_multisplit(const TileJob<K, S>& job, unsigned char* smem,
+                                                         uint64_t* s_bar, uint32_t& parity) {
+  using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
+  using SW = StatusWord<S>;
+  constexpr int TILE = G::kTile;
+  constexpr int WARPS = G::kWarps;
+  constexpr uint32_t FULL = 0xFFFFFFFFu;
+  static_assert((size_t)WARPS * kRadix <= (size_t)kNibbleBins * G::kCntRow, "warp counters fit the counter area");
+  K* s_keys = reinterpret_cast<K*>(smem + G::kKeysOff);
+  uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + G::kValsOff);
+  uint32_t* s_wh = reinterpret_cast<uint32_t*>(smem + G::kCntOff);  // [WARPS][256]
+  S* s_base = reinterpret_cast<S*>(smem + G::kBinBaseOff);
+  uint32_t* s_tstart = reinterpret_cast<uint32_t*>(smem + G::kBinStartOff);
+  uint32_t* s_tcount = reinterpret_cast<uint32_t*>(smem + G::kBinEndOff);
+  uint32_t* s_abort = reinterpret_cast<uint32_t*>(smem + G::kAbortOff);
+
+  const K* in = job.in;
+  K* out = job.out;
+  const uint32_t* vin = job.vin;
+  uint32_t* vout = job.vout;
+  const uint32_t shift = job.shift;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+  const uint32_t tile = job.tile;
+  const size_t tile_base = (size_t)tile * TILE;
+  const uint32_t tile_n = (uint32_t)min((size_t)TILE, job.n - tile_base);
+  const bool full = tile_n == (uint32_t)TILE;
+  if (tid == 0) *s_abort = 0;
+  for (uint32_t i = tid; i < (uint32_t)(WARPS * kRadix); i += BLOCK) s_wh[i] = 0;
+
+  // tile -> shared memory (bulk copy; plain loads for the ragged end)
+  const bool tma_ok = ((reinterpret_cast<uintptr_t>(in) & 15u) == 0) &&
+                      (!HAS_VALS || (reinterpret_cast<uintptr_t>(vin) & 15u) == 0);
+  uint32_t loaded = 0;
+  if (tma_ok) {
+    const uint32_t kbulk = (tile_n * (uint32_t)sizeof(K)) & ~15u;
+    const uint32_t vbulk = HAS_VALS ? ((tile_n * 4u) & ~15u) : 0u;
+    if (tid == 0) {
+      fence_proxy_async();
+      mbar_arrive_expect_tx(s_bar, kbulk + vbulk);
+      if (kbulk) bulk_load_g2s(s_keys, in + tile_base, kbulk, s_bar);
+      if (HAS_VALS && vbulk) bulk_load_g2s(s_vals, vin + tile_base, vbulk, s_bar);
+    }
+    loaded = kbulk / (uint32_t)sizeof(K);
+    if (HAS_VALS)
+      for (uint32_t i = vbulk / 4u + tid; i < tile_n; i += BLOCK) s_vals[i] = vin[tile_base + i];
+  } else if (HAS_VALS) {
+    for (uint32_t i = tid; i < tile_n; i += BLOCK) s_vals[i] = vin[tile_base + i];
+  }
+  for (uint32_t i = loaded + tid; i < tile_n; i += BLOCK) s_keys[i] = in[tile_base + i];
+  if (tma_ok) {
+    if (!mbar_wait_bounded(s_bar, parity, job.err)) *s_abort = 1;
+    parity ^= 1u;
+  }
+  __syncthreads();
+
+  // rank within the warp
+  const uint32_t dsel = 0x4440u | ((shift >> 3) & 3u);
+  const bool dupper = shift >= 32;
+  const uint32_t lt = lanemask_lt();
+  const uint32_t wbase = warp * ITEMS * 32;
+  uint32_t* wh = s_wh + warp * kRadix;
+  K k[ITEMS];
+  uint32_t v[HAS_VALS ? ITEMS : 1];
+  uint32_t rk[(ITEMS + 1) / 2];  // in-warp ranks (< 32 * ITEMS), two 16-bit halves per word
+#pragma unroll
+  for (int q = 0; q < (ITEMS + 1) / 2; ++q) rk[q] = 0;
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
+    const bool valid = full || idx < tile_n;
+    k[j] = valid ? to_ordered(s_keys[idx], job.tin) : (K)0;
+    if (HAS_VALS) v[j] = valid ? s_vals[idx] : 0u;
+    const uint32_t d = digit8(k[j], dsel, dupper);
+    uint32_t peers = match_digit8(d);
+    if (!full) {
+      const uint32_t vm = __ballot_sync(FULL, valid);
+      peers &= valid ? vm : ~vm;
+    }
+    const uint32_t leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader && valid) {
+      base = wh[d];
+      wh[d] = base + __popc(peers);
+    }
+    base = __shfl_sync(FULL, base, leader);
+    rk[j / 2] |= (base + __popc(peers & lt)) << (16 * (j % 2));
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // per bin: exclusive scan over warps, tile count, publish
+  if (tid < (uint32_t)kRadix) {
+    uint32_t sum = 0;
+#pragma unroll 4
+    for (int w = 0; w < WARPS; ++w) {
+      const uint32_t c = s_wh[w * kRadix + tid];
+      s_wh[w * kRadix + tid] = sum;
+      sum += c;
+    }
+    s_tcount[tid] = sum;
+    S* st = job.status + (size_t)tile * kRadix + tid;
+    st_relaxed_gpu(st, (S)((tile == 0 ? SW::kIncl : SW::kAgg) | (S)sum));
+  }
+  __syncthreads();
+  if (warp == 0) {  // exclusive scan of the 256 tile counts, 8 bins per lane
+    uint32_t c[kRadix / 32];
+    uint32_t local = 0;
+#pragma unroll
+    for (int i = 0; i < kRadix / 32; ++i) {
+      c[i] = s_tcount[lane * (kRadix / 32) + i];
+      local += c[i];
+    }
+    uint32_t incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(FULL, incl, o);
+      if (lane >= (uint32_t)o) incl += t;
+    }
+    uint32_t run = incl - local;
+#pragma unroll
+    for (int i = 0; i < kRadix / 32; ++i) {
+      s_tstart[lane * (kRadix / 32) + i] = run;
+      run += c[i];
+    }
+  }
+  __syncthreads();
+  if (tid < (uint32_t)kRadix) {  // fold the tile offset of each bin into the warp offsets
+    const uint32_t ts = s_tstart[tid];
+#pragma unroll 4
+    for (int w = 0; w < WARPS; ++w) s_wh[w * kRadix + tid] += ts;
+  }
+  __syncthreads();
+
+  // stage keys at their in-tile sorted position; then the look-back
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
+    if (full || idx < tile_n) {
+      const uint32_t pos = wh[digit8(k[j], dsel, dupper)] + ((rk[j / 2] >> (16 * (j % 2))) & 0xFFFFu);
+      s_keys[pos] = k[j];
+      if (HAS_VALS) s_vals[pos] = v[j];
+    }
+  }
+  if (tid < (uint32_t)kRadix) {
+    const uint32_t count = s_tcount[tid];
+    S excl = 0;
+    if (tile > 0) {
+      const S* base = job.status + tid;
+      long long t = (long long)tile - 1;
+      uint32_t spins = 0;
+      bool done = false;
+      while (!done) {
+        S sw[kLookbackWidth];
+#pragma unroll
+        for (int i = 0; i < kLookbackWidth; ++i)
+          sw[i] = (t - i >= 0) ? ld_relaxed_gpu(base + (size_t)(t - i) * kRadix) : (S)SW::kIncl;
+        int used = 0;
+#pragma unroll
+        for (int i = 0; i < kLookbackWidth; ++i) {
+          if (done || used != i) break;
+          const uint32_t flag = (uint32_t)(sw[i] >> SW::kShift);
+          if (flag == 0) break;
+          excl += sw[i] & SW::kMask;
+          ++used;
+          if (flag == 2u) done = true;
+        }
+        t -= used;
+        if (!done && used == 0 && ++spins > kSpinLimit) {
+          raise_error(job.err, DEVERR_LOOKBACK_TIMEOUT);
+          *s_abort = 1;
+          break;
+        }
+      }
+      S* st = job.status + (size_t)tile * kRadix + tid;
+      st_relaxed_gpu(st, (S)(SW::kIncl | (S)(excl + count)));
+    }
+    s_base[tid] = (S)job.bin_start[tid] + excl - (S)s_tstart[tid];
+  }
+  __syncthreads();
+
+  // write out in bin-contiguous runs
+  if (*s_abort) return;
+  const S n_out = (S)job.n;
+  auto scatter = [&](auto transform) {
+    if (full) {
+#pragma unroll 4
+      for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t i = (uint32_t)j * BLOCK + tid;
+        const K key = s_keys[i];
+        const S o = s_base[digit8(key, dsel, dupper)] + i;
+        if (o < n_out) {
+          out[o] = transform(key);
+          if (HAS_VALS) vout[o] = s_vals[i];
+        }
+      }
+    } else {
+      for (uint32_t i = tid; i < tile_n; i += BLOCK) {
+        const K key = s_keys[i];
+        const S o = s_base[digit8(key, dsel, dupper)] + i;
+        if (o < n_out) {
+          out[o] = transform(key);
+          if (HAS_VALS) vout[o] = s_vals[i];
+        }
+      }
+    }
+  };
+  if (job.tout)
+    scatter([](K x) { return from_ordered(x, true); });
+  else
+    scatter([](K x) { return x; });
+}
+
 }  // namespace os
 }  // namespace pa
