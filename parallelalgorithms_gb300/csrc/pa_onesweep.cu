@@ -122,13 +122,14 @@ GeomChoice active_geometry() {
   return kGeomU64Kv[geometry_index(3)];
 }
 
-// Ranking method of the uint32 keys-only pass: the in-tile counting sort
-// (default) or the warp multisplit (PA_ONESWEEP_RANK=multisplit).
+// Ranking method of a pass: the warp multisplit (default; faster on GB300,
+// profiles/onesweep_pass_u32_50m.md) or the in-tile counting sort
+// (PA_ONESWEEP_RANK=counting).
 bool use_multisplit() {
   static int v = -1;
   if (v < 0) {
     const char* e = std::getenv("PA_ONESWEEP_RANK");
-    v = (e && std::strcmp(e, "multisplit") == 0) ? 1 : 0;
+    v = (e && std::strcmp(e, "counting") == 0) ? 0 : 1;
   }
   return v == 1;
 }
@@ -150,9 +151,7 @@ cudaError_t launch_g2(const OnesweepArgs& a, cudaStream_t stream) {
 
 template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S>
 cudaError_t launch_g(const OnesweepArgs& a, cudaStream_t stream) {
-  if constexpr (sizeof(K) == 4 && !HAS_VALS) {
-    if (use_multisplit()) return launch_g2<K, HAS_VALS, BLOCK, ITEMS, MINB, S, true>(a, stream);
-  }
+  if (use_multisplit()) return launch_g2<K, HAS_VALS, BLOCK, ITEMS, MINB, S, true>(a, stream);
   return launch_g2<K, HAS_VALS, BLOCK, ITEMS, MINB, S, false>(a, stream);
 }
 
