@@ -240,7 +240,10 @@ typedef struct pa_serve_config {
   int max_batch_requests;   /* 32-bit sorts coalesced into one launch: 0 = 256 */
   int no_coalesce;          /* 1: every request runs alone */
   int num_streams;          /* 0 = 4 */
-  int reserved[4];          /* must be zero */
+  int reserve_mib;          /* device memory (MiB, at most the budget) mapped into the
+                               server's pool at creation, so that admissions do not wait
+                               for the pool to map memory; 0 = map on demand */
+  int reserved[3];          /* must be zero */
 } pa_serve_config;
 typedef struct pa_server pa_server;
 

@@ -320,8 +320,23 @@ PlanDev device_view(const HostPlan& hp, char* dev, uint32_t* keys, uint32_t* tmp
   return d;
 }
 
-cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s) {
+size_t plan_image_bytes(const HostPlan& hp) {
+  return hp.o_large + std::max<size_t>(hp.large.size(), 1) * sizeof(LargeSeg);
+}
+
+cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s, void* pinned_staging) {
   cudaError_t e = cudaSuccess;
+  if (pinned_staging) {
+    char* img = static_cast<char*>(pinned_staging);
+    const size_t bytes = plan_image_bytes(hp);
+    std::memset(img, 0, bytes);
+    if (!hp.items.empty()) std::memcpy(img + hp.o_items, hp.items.data(), hp.items.size() * sizeof(Item));
+    std::memcpy(img + hp.o_off, hp.off.data(), hp.off.size() * 8);
+    if (!hp.large.empty()) std::memcpy(img + hp.o_large, hp.large.data(), hp.large.size() * sizeof(LargeSeg));
+    e = cudaMemcpyAsync(dev, img, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dev + hp.o_err, 0, 256, s);
+    return e;
+  }
   if (!hp.items.empty())
     e = cudaMemcpyAsync(dev + hp.o_items, hp.items.data(), hp.items.size() * sizeof(Item), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)

@@ -82,7 +82,13 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
 // Pointers of a device block laid out by `hp` (keys / tmp: the batch's keys).
 PlanDev device_view(const HostPlan& hp, char* dev, uint32_t* keys, uint32_t* tmp);
 // Copies the queue, offsets and segment table into the block; clears its error word.
-cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s);
+// With `pinned_staging` (page-locked, at least plan_image_bytes(hp) bytes, left
+// untouched by the caller until the copy has run) the three tables go up in
+// one asynchronous copy; without it they are copied from the plan's own
+// pageable vectors, which makes the runtime wait for the stream first.
+cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s, void* pinned_staging = nullptr);
+// Bytes of the block's leading image (queue, offsets, segment table).
+size_t plan_image_bytes(const HostPlan& hp);
 // Persistent grid for the plan's kernel on the current device.
 unsigned plan_grid(const HostPlan& hp);
 // Clears the per-run state and launches the persistent kernel.

@@ -9,13 +9,19 @@
 // 799-892 with MemoryUsage.cpp:20-87, which here becomes admission by free
 // HBM against a configured budget).
 //
-// Each admitted unit runs on one of several streams: host->device copies of
-// its keys, its kernels, device->host copies of its results, all in one
-// stream-ordered allocation (cudaMallocAsync / cudaFreeAsync, so admission
-// never synchronises the device), then an event the scheduler polls.
-// Units on different streams overlap: copies of one with kernels of another.
+// Each admitted unit runs on the least busy of several streams: host->device
+// copies of its keys, its kernels, device->host copies of its results, all in
+// one stream-ordered allocation from the server's own memory pool (so
+// admission never synchronises the device), then an event the scheduler
+// polls.  Units on different streams overlap: copies of one with kernels of
+// another.  The pool does not let a unit reuse memory that a unit on another
+// stream freed but whose work is still running (that reuse would make the
+// runtime chain the two streams and serialise the units); it reuses memory
+// once the freeing unit's work has completed, and keeps what it has mapped
+// until the server is destroyed.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -41,6 +47,8 @@ struct UnitState {
   cudaEvent_t ev = nullptr;
   char* dmem = nullptr;
   uint32_t* err_host = nullptr;  // pinned word the unit's device error word is copied to
+  void* staging = nullptr;       // pinned image of a batched unit's plan tables
+  void* result_host = nullptr;   // pinned landing place of a select / histogram result
   cudaError_t launch_error = cudaSuccess;
   std::unique_ptr<seg::HostPlan> plan;
 };
@@ -64,20 +72,28 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 class GpuBackend {
  public:
-  GpuBackend(int lanes) {
+  explicit GpuBackend(int lanes) {
     cudaGetDevice(&device_);
-    // Keep memory freed by finished units in the process's stream-ordered pool
-    // instead of returning it to the driver at every synchronisation.
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, device_) == cudaSuccess) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device_;
+    if (cudaMemPoolCreate(&pool_, &props) == cudaSuccess) {
       uint64_t keep = ~0ull;
-      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      int no = 0, yes = 1;
+      cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep);
+      cudaMemPoolSetAttribute(pool_, cudaMemPoolReuseAllowInternalDependencies, &no);
+      cudaMemPoolSetAttribute(pool_, cudaMemPoolReuseAllowOpportunistic, &yes);
+      cudaMemPoolSetAttribute(pool_, cudaMemPoolReuseFollowEventDependencies, &yes);
+    } else {
+      pool_ = nullptr;
     }
     cudaGetLastError();
     for (int i = 0; i < lanes; ++i) {
       cudaStream_t s;
       cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
       streams_.push_back(s);
+      lane_units_.push_back(0);
     }
   }
   ~GpuBackend() {
@@ -85,16 +101,39 @@ class GpuBackend {
       cudaStreamSynchronize(s);
       cudaStreamDestroy(s);
     }
-    for (auto* w : pinned_words_) cudaFreeHost(w);
+    if (pool_) cudaMemPoolDestroy(pool_);
+    for (const auto& b : pinned_) cudaFreeHost(b.first);
+  }
+  bool ok() const { return pool_ != nullptr && !streams_.empty(); }
+
+  // Maps `bytes` into the pool now (one allocation, freed at once; the pool
+  // keeps what it mapped), so later admissions reuse it instead of waiting
+  // for the driver to map memory.
+  cudaError_t reserve(size_t bytes) {
+    if (!bytes) return cudaSuccess;
+    void* p = nullptr;
+    cudaStream_t s = streams_[0];
+    cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, pool_, s);
+    if (e == cudaSuccess) e = cudaFreeAsync(p, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) cudaGetLastError();
+    return e;
   }
   int device() const { return device_; }
 
+  // Device memory free to the driver plus what the server's pool holds mapped
+  // but unused (it keeps memory of finished units for reuse).
   size_t free_bytes() {
     size_t f = 0, t = 0;
     if (cudaMemGetInfo(&f, &t) != cudaSuccess) {
       cudaGetLastError();
       return 0;
     }
+    uint64_t reserved = 0, used = 0;
+    if (pool_ && cudaMemPoolGetAttribute(pool_, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+        cudaMemPoolGetAttribute(pool_, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+      f += (size_t)(reserved - used);
+    cudaGetLastError();
     return f;
   }
 
@@ -122,13 +161,25 @@ class GpuBackend {
   void launch(Unit& u) {
     auto* st = new UnitState();
     u.state = st;
-    st->lane = next_lane_++ % (int)streams_.size();
+    // the lane with the fewest units in flight; ties go round robin
+    const int lanes = (int)streams_.size();
+    st->lane = next_lane_;
+    for (int i = 1; i < lanes; ++i) {
+      const int c = (next_lane_ + i) % lanes;
+      if (lane_units_[c] < lane_units_[st->lane]) st->lane = c;
+    }
+    next_lane_ = (st->lane + 1) % (int)streams_.size();
+    ++lane_units_[st->lane];
     u.lane = st->lane;
     cudaStream_t s = streams_[st->lane];
-    st->err_host = take_word();
+    st->err_host = static_cast<uint32_t*>(take_pinned(64));
+    if (!st->err_host) {
+      st->launch_error = cudaErrorMemoryAllocation;
+      return;
+    }
     *st->err_host = 0;
     cudaError_t e = cudaEventCreateWithFlags(&st->ev, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&st->dmem), u.bytes, s);
+    if (e == cudaSuccess) e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&st->dmem), u.bytes, pool_, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(st->dmem, 0, 256, s);  // error word + result slot
     if (e == cudaSuccess) e = u.batched ? launch_batch(u, st, s) : launch_single(u, st, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(st->err_host, st->dmem, 4, cudaMemcpyDeviceToHost, s);
@@ -158,13 +209,29 @@ class GpuBackend {
   void finish(Unit& u) {
     auto* st = static_cast<UnitState*>(u.state);
     int status = PA_OK;
+    // after a failed launch, copies enqueued before the failure may still
+    // read the request's buffers or the staging block: let them finish
+    if (st->launch_error != cudaSuccess) {
+      cudaStreamSynchronize(streams_[st->lane]);
+      cudaGetLastError();
+    }
     if (st->launch_error != cudaSuccess)
       status = st->launch_error == cudaErrorMemoryAllocation ? PA_ERR_OOM : PA_ERR_CUDA;
     else if (*st->err_host)
       status = PA_ERR_TIMEOUT;
+    // results land in page-locked memory first (a device-to-host copy into the
+    // caller's pageable array would make the launching thread wait for the
+    // unit's work); they move to the caller's array now that the work is done
+    if (status == PA_OK && st->result_host && u.reqs.size() == 1) {
+      const Request* r = u.reqs[0];
+      std::memcpy(user_of(r)->result, st->result_host, r->op == OP_SELECT ? 8 : 256 * 8);
+    }
     for (Request* r : u.reqs) r->status = status;
     if (st->ev) cudaEventDestroy(st->ev);
-    give_word(st->err_host);
+    --lane_units_[st->lane];
+    give_pinned(st->err_host);
+    give_pinned(st->staging);
+    give_pinned(st->result_host);
     delete st;
     u.state = nullptr;
   }
@@ -198,17 +265,21 @@ class GpuBackend {
       e = enqueue_sort(sc, keys, tmp, nullptr, nullptr, r->n, (int)kb, false, err, s);
       if (e == cudaSuccess && host) e = cudaMemcpyAsync(q->keys, keys, r->n * kb, cudaMemcpyDeviceToHost, s);
     } else if (r->op == OP_SELECT) {
+      st->result_host = take_pinned(8);
+      if (!st->result_host) return cudaErrorMemoryAllocation;
       const size_t cap = r->n / 4 + 1024;
       void* cand = base + off;
       off += align256(cap * kb);
       void* work = base + off;
       e = launch_select(keys, r->n, q->k, (int)kb, cand, cap, work, result, err, s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(q->result, result, 8, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(st->result_host, result, 8, cudaMemcpyDeviceToHost, s);
     } else {
+      st->result_host = take_pinned(256 * 8);
+      if (!st->result_host) return cudaErrorMemoryAllocation;
       auto* counts = reinterpret_cast<unsigned long long*>(base + off);
       e = cudaMemsetAsync(counts, 0, 256 * 8, s);
       if (e == cudaSuccess) e = launch_digit_counts(keys, r->n, (int)kb, 1, 8, q->shift, 0, false, counts, s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(q->result, counts, 256 * 8, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(st->result_host, counts, 256 * 8, cudaMemcpyDeviceToHost, s);
     }
     return e;
   }
@@ -222,6 +293,10 @@ class GpuBackend {
     st->plan.reset(new seg::HostPlan());
     pa_segsort_config cfg{};
     if (seg::build_host_plan(off.data(), u.reqs.size(), &cfg, st->plan.get()) != PA_OK) return cudaErrorInvalidValue;
+    // the plan tables go up from page-locked memory: a copy from pageable
+    // memory would make this thread wait for the stream's earlier copies
+    st->staging = take_pinned(seg::plan_image_bytes(*st->plan));
+    if (!st->staging) return cudaErrorMemoryAllocation;
     char* base = st->dmem;
     uint32_t* keys = reinterpret_cast<uint32_t*>(base + 256);
     uint32_t* tmp = reinterpret_cast<uint32_t*>(base + 256 + align256(total * 4));
@@ -231,7 +306,7 @@ class GpuBackend {
       pa_request* q = user_of(u.reqs[i]);
       e = cudaMemcpyAsync(keys + off[i], q->keys, u.reqs[i]->n * 4, cudaMemcpyDefault, s);
     }
-    if (e == cudaSuccess) e = seg::upload_plan(*st->plan, plan, s);
+    if (e == cudaSuccess) e = seg::upload_plan(*st->plan, plan, s, st->staging);
     if (e == cudaSuccess) {
       seg::PlanDev pd = seg::device_view(*st->plan, plan, keys, tmp);
       pd.err = reinterpret_cast<uint32_t*>(base);  // the unit's error word
@@ -244,36 +319,49 @@ class GpuBackend {
     return e;
   }
 
-  uint32_t* take_word() {
-    std::lock_guard<std::mutex> lk(mu_);
-    if (free_words_.empty()) {
-      uint32_t* w = nullptr;
-      if (cudaMallocHost(&w, 64) != cudaSuccess) {
-        cudaGetLastError();
-        static uint32_t fallback;
-        return &fallback;
-      }
-      pinned_words_.push_back(w);
-      return w;
-    }
-    uint32_t* w = free_words_.back();
-    free_words_.pop_back();
-    return w;
+  // Page-locked host blocks in power-of-two size classes, kept for reuse
+  // until the server is destroyed (freeing page-locked memory synchronises
+  // the device).  Returns nullptr if the allocation fails.
+  static int size_class(size_t bytes) {
+    int c = 6;
+    while (((size_t)1 << c) < bytes) ++c;
+    return c;
   }
-  void give_word(uint32_t* w) {
+  void* take_pinned(size_t bytes) {
+    const int c = size_class(bytes);
     std::lock_guard<std::mutex> lk(mu_);
-    for (auto* p : pinned_words_)
-      if (p == w) {
-        free_words_.push_back(w);
+    auto& fl = free_pinned_[c];
+    if (!fl.empty()) {
+      void* p = fl.back();
+      fl.pop_back();
+      return p;
+    }
+    void* p = nullptr;
+    if (cudaMallocHost(&p, (size_t)1 << c) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    pinned_.push_back({p, c});
+    return p;
+  }
+  void give_pinned(void* p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(mu_);
+    for (const auto& b : pinned_)
+      if (b.first == p) {
+        free_pinned_[b.second].push_back(p);
         return;
       }
   }
 
   int device_ = 0;
+  cudaMemPool_t pool_ = nullptr;
   std::vector<cudaStream_t> streams_;
+  std::vector<int> lane_units_;
   int next_lane_ = 0;
   std::mutex mu_;
-  std::vector<uint32_t*> pinned_words_, free_words_;
+  std::vector<std::pair<void*, int>> pinned_;
+  std::vector<void*> free_pinned_[64];
 };
 
 }  // namespace
@@ -336,6 +424,7 @@ int pa_server_create(const pa_serve_config* cfg, pa_server** out) {
   if (cfg) c = *cfg;
   for (int r : c.reserved)
     if (r) return record_error(PA_ERR_ARG, "pa_serve_config.reserved must be zero");
+  if (c.reserve_mib < 0) return record_error(PA_ERR_ARG, "pa_serve_config.reserve_mib is negative");
   Config sc;
   if (c.hbm_budget_bytes) sc.budget_bytes = c.hbm_budget_bytes;
   if (c.max_inflight > 0) sc.max_inflight = c.max_inflight;
@@ -344,6 +433,17 @@ int pa_server_create(const pa_serve_config* cfg, pa_server** out) {
   const int lanes = c.num_streams > 0 ? c.num_streams : 4;
   auto* s = new pa_server();
   s->backend.reset(new GpuBackend(lanes));
+  if (!s->backend->ok()) {
+    delete s;
+    return record_error(PA_ERR_CUDA, "could not create the server's memory pool or streams");
+  }
+  if (c.reserve_mib > 0) {
+    const size_t want = std::min((size_t)c.reserve_mib << 20, sc.budget_bytes);
+    if (s->backend->reserve(want) != cudaSuccess) {
+      delete s;
+      return record_error(PA_ERR_OOM, "could not map reserve_mib of device memory into the server's pool");
+    }
+  }
   s->sched.reset(new Scheduler<GpuBackend>(*s->backend, sc, [s](Request* r) { on_done(s, r); }));
   s->worker = std::thread(worker_loop, s, s->backend->device());
   *out = s;

@@ -36,7 +36,7 @@ class PaRequest(ctypes.Structure):
 class ServeConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_inflight", ctypes.c_int),
                 ("max_batch_requests", ctypes.c_int), ("no_coalesce", ctypes.c_int),
-                ("num_streams", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+                ("num_streams", ctypes.c_int), ("reserve_mib", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 @dataclass
@@ -73,10 +73,10 @@ class Request:
 
 class Server:
     def __init__(self, budget_bytes: int = 64 << 30, max_inflight: int = 4, max_batch_requests: int = 256,
-                 coalesce: bool = True, num_streams: int = 4):
+                 coalesce: bool = True, num_streams: int = 4, reserve_bytes: int = 0):
         cfg = ServeConfig(hbm_budget_bytes=budget_bytes, max_inflight=max_inflight,
                           max_batch_requests=max_batch_requests, no_coalesce=0 if coalesce else 1,
-                          num_streams=num_streams)
+                          num_streams=num_streams, reserve_mib=(reserve_bytes + (1 << 20) - 1) >> 20)
         h = ctypes.c_void_p()
         call("pa_server_create", ctypes.byref(cfg), ctypes.byref(h))
         self._h = h
@@ -198,6 +198,67 @@ def run_plain(specs: list[Spec], bufs, per_call: list | None = None) -> tuple[li
         else:
             out = np.zeros(256, np.uint64)
             call(f"pa_hist_one_byte_{kk}", P(buf.ctypes.data), s.n, 0, P(out.ctypes.data), None)
+            results.append(out)
+        dt = time.perf_counter() - t0
+        total += dt
+        if per_call is not None:
+            per_call.append(dt)
+    return results, total
+
+
+def device_copies(bufs) -> list:
+    """(work, pristine) CUDA tensor pairs holding each request's keys in HBM,
+    for the device-resident forms of the stream."""
+    import torch
+    out = []
+    for (_, _, src) in bufs:
+        t = torch.from_numpy(src.view(np.int32 if src.dtype == np.uint32 else np.int64)).cuda()
+        out.append((torch.empty_like(t), t))
+    torch.cuda.synchronize()
+    return out
+
+
+def run_served_device(server: Server, specs: list[Spec], dev, rate: float | None, seed: int = 7) -> list[Request]:
+    """run_served with the keys already in HBM (restored before the first submission)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    for work, src in dev:
+        work.copy_(src)
+    torch.cuda.synchronize()
+    reqs = [Request(s.op, work, k=s.k) for s, (work, _) in zip(specs, dev)]
+    t_next = time.perf_counter()
+    for r in reqs:
+        if rate:
+            t_next += rng.exponential(1.0 / rate)
+            while time.perf_counter() < t_next:
+                pass
+        server.submit(r)
+    server.drain()
+    return reqs
+
+
+def run_plain_device(specs: list[Spec], dev, per_call: list | None = None) -> tuple[list, float]:
+    """run_plain with the keys already in HBM: one synchronous call per request
+    on the device buffer (restoring it is not timed)."""
+    import torch
+    results = []
+    total = 0.0
+    for s, (work, src) in zip(specs, dev):
+        work.copy_(src)
+        torch.cuda.synchronize()
+        kk = "u32" if s.key_kind == KEY_U32 else "u64"
+        ptr = P(work.data_ptr())
+        t0 = time.perf_counter()
+        if s.op == REQ_SORT:
+            call(f"pa_sort_{kk}", ptr, None, s.n, None)
+            results.append(None)
+        elif s.op == REQ_SELECT:
+            out = np.zeros(1, np.uint64)
+            call(f"pa_select_{kk}", ptr, s.n, s.k, P(out.ctypes.data), None)
+            results.append(out)
+        else:
+            out = np.zeros(256, np.uint64)
+            call(f"pa_hist_one_byte_{kk}", ptr, s.n, 0, P(out.ctypes.data), None)
             results.append(out)
         dt = time.perf_counter() - t0
         total += dt
