@@ -55,6 +55,9 @@ def _stale() -> bool:
     if not LIB.exists():
         return True
     newest = max(p.stat().st_mtime for p in list(CSRC.iterdir()) + [INCLUDE / "pa_gpu.h", Path(__file__)])
+    flags = LIB.with_suffix(".flags")
+    if (flags.read_text() if flags.exists() else "") != os.environ.get("PA_NVCC_FLAGS", ""):
+        return True
     return LIB.stat().st_mtime < newest
 
 
@@ -64,6 +67,8 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
         return LIB
     BUILD.mkdir(exist_ok=True)
     extra = ["-Xptxas", "-v"] if verbose_ptxas else []
+    # PA_NVCC_FLAGS: extra compiler flags (e.g. -D tuning switches of the kernels)
+    extra += os.environ.get("PA_NVCC_FLAGS", "").split()
     srcs = _sources()
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
@@ -74,6 +79,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    LIB.with_suffix(".flags").write_text(os.environ.get("PA_NVCC_FLAGS", ""))
     return LIB
 
 

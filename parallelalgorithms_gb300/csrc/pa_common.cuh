@@ -8,6 +8,9 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+#include <utility>
+
 namespace pa {
 
 // ---------------------------------------------------------------------------
@@ -176,5 +179,16 @@ __device__ __forceinline__ uint4 ld_stream_v4(const void* p) {
 }
 
 __host__ __device__ constexpr inline size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
+
+// Calls f(std::integral_constant<int, i>{}) for i = 0 .. N-1, unrolled at
+// compile time (so that per-item choices can be made with if constexpr).
+template <typename F, int... I>
+__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
 
 }  // namespace pa

@@ -100,7 +100,7 @@ __global__ void final_copy_kernel(K* keys_a, const K* keys_b, uint32_t* vals_a, 
 struct GeomChoice {
   int block, items, minb;
 };
-constexpr GeomChoice kGeomU32[] = {{512, 16, 2}, {256, 16, 4}, {384, 16, 3}, {1024, 8, 1}, {512, 8, 3}};
+constexpr GeomChoice kGeomU32[] = {{384, 16, 3}, {512, 16, 2}, {256, 16, 4}, {1024, 8, 1}, {512, 8, 3}};
 constexpr GeomChoice kGeomU32Kv[] = {{512, 12, 2}, {256, 12, 4}, {512, 8, 3}};
 constexpr GeomChoice kGeomU64[] = {{256, 12, 4}, {512, 12, 2}, {512, 8, 3}};
 constexpr GeomChoice kGeomU64Kv[] = {{256, 12, 3}, {256, 8, 4}, {512, 8, 2}};
@@ -122,18 +122,6 @@ GeomChoice active_geometry() {
   return kGeomU64Kv[geometry_index(3)];
 }
 
-// Ranking method of a pass: the warp multisplit (default; faster on GB300,
-// profiles/onesweep_pass_u32_50m.md) or the in-tile counting sort
-// (PA_ONESWEEP_RANK=counting).
-bool use_multisplit() {
-  static int v = -1;
-  if (v < 0) {
-    const char* e = std::getenv("PA_ONESWEEP_RANK");
-    v = (e && std::strcmp(e, "counting") == 0) ? 0 : 1;
-  }
-  return v == 1;
-}
-
 template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S, bool MS>
 cudaError_t launch_g2(const OnesweepArgs& a, cudaStream_t stream) {
   using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
@@ -147,6 +135,20 @@ cudaError_t launch_g2(const OnesweepArgs& a, cudaStream_t stream) {
   const size_t tiles = ceil_div(a.n, (size_t)G::kTile);
   kern<<<(unsigned)tiles, BLOCK, G::kBytes, stream>>>(a);
   return cudaGetLastError();
+}
+
+// Ranking method of a pass: the warp multisplit (default) or the in-tile
+// counting sort (PA_ONESWEEP_RANK=counting).  A persistent form of the
+// multisplit pass that copied each CTA's next tile in while it worked on the
+// current one was measured slower on GB300 (tickets taken early make
+// successors wait in the look-back) and is not built.
+bool use_multisplit() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("PA_ONESWEEP_RANK");
+    v = (e && std::strcmp(e, "counting") == 0) ? 0 : 1;
+  }
+  return v == 1;
 }
 
 template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S>

@@ -13,7 +13,10 @@ namespace os {
 constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kNibbleBins = 16;
-constexpr int kLookbackWidth = 4;  // predecessor tiles read per round trip
+#ifndef PA_LOOKBACK_WIDTH
+#define PA_LOOKBACK_WIDTH 4
+#endif
+constexpr int kLookbackWidth = PA_LOOKBACK_WIDTH;  // predecessor tiles read per round trip
 
 template <typename S>
 struct StatusWord;
@@ -356,10 +359,13 @@ __device__ __forceinline__ void onesweep_tile(const TileJob<K, S>& job, unsigned
           if (flag == 2u) done = true;
         }
         t -= used;
-        if (!done && used == 0 && ++spins > kSpinLimit) {
-          raise_error(job.err, DEVERR_LOOKBACK_TIMEOUT);
-          *s_abort = 1;
-          break;
+        if (!done && used == 0) {
+          ++spins;
+          if (spins > kSpinLimit || ((spins & 1023u) == 0 && ld_relaxed_gpu(job.err) != 0)) {
+            raise_error(job.err, DEVERR_LOOKBACK_TIMEOUT);
+            *s_abort = 1;
+            break;
+          }
         }
       }
       S* st = job.status + (size_t)tile * kRadix + tid;
@@ -430,31 +436,88 @@ __device__ __forceinline__ uint32_t match_digit8(uint32_t d) {
   return peers;
 }
 
-// The same tile job as onesweep_tile, ranked by warp multisplit instead of
-// the in-tile counting sort: warp w owns the contiguous run
-// [w * 32 * ITEMS, (w + 1) * 32 * ITEMS) of the tile, lane l its items
+// Shared-memory places one multisplit tile uses: the tile buffer (keys and
+// payloads) and the per-tile scratch (per-warp bin counters, bin bases and
+// starts, tile bin counts, abort flag).
+template <typename K, typename S>
+struct TileSmem {
+  K* keys;
+  uint32_t* vals;
+  uint32_t* wh;      // [warps][256] counters (and [warps][256] match words)
+  S* base;           // [256] global base of each bin for this tile
+  uint32_t* tstart;  // [256] first in-tile position of each bin
+  uint32_t* tcount;  // [256] keys of each bin in the tile
+  uint32_t* abort;
+};
+
+// Whether a pass can bulk-copy its tiles (16-byte aligned key and payload
+// arrays); otherwise every key is read with plain loads.
+template <typename K, bool HAS_VALS, typename S>
+__device__ __forceinline__ bool tile_tma_ok(const TileJob<K, S>& job) {
+  return ((reinterpret_cast<uintptr_t>(job.in) & 15u) == 0) &&
+         (!HAS_VALS || (reinterpret_cast<uintptr_t>(job.vin) & 15u) == 0);
+}
+
+// Starts the bulk copy of tile `tile` into `keys` / `vals`, completing on
+// `bar` (one thread calls it; the 16-byte multiple head of the tile only, the
+// body reads the ragged rest).  Nothing is issued for a pass that cannot
+// bulk-copy.
+template <typename K, bool HAS_VALS, int TILE, typename S>
+__device__ __forceinline__ void tile_issue_load(const TileJob<K, S>& job, uint32_t tile, K* keys, uint32_t* vals,
+                                                uint64_t* bar) {
+  if (!tile_tma_ok<K, HAS_VALS>(job)) return;
+  const size_t tile_base = (size_t)tile * TILE;
+  const uint32_t tile_n = (uint32_t)min((size_t)TILE, job.n - tile_base);
+  const uint32_t kbulk = (tile_n * (uint32_t)sizeof(K)) & ~15u;
+  const uint32_t vbulk = HAS_VALS ? ((tile_n * 4u) & ~15u) : 0u;
+  fence_proxy_async();
+  mbar_arrive_expect_tx(bar, kbulk + vbulk);
+  if (kbulk) bulk_load_g2s(keys, job.in + tile_base, kbulk, bar);
+  if (HAS_VALS && vbulk) bulk_load_g2s(vals, job.vin + tile_base, vbulk, bar);
+}
+
+// Tuning switches of the multisplit ranking (compile-time):
+//   PA_MATCH_ATOMIC_OR = 1: peers are found through shared memory instead of
+//     ballots: each lane ORs its lane bit into its warp's word for its digit
+//     and reads the word back; the group's leader clears it again.
+#ifndef PA_MATCH_ATOMIC_OR
+#define PA_MATCH_ATOMIC_OR 0
+#endif
+constexpr int kMatchWords = PA_MATCH_ATOMIC_OR ? 2 : 1;  // [warps][256] word arrays in TileSmem::wh
+
+// Applies the float order transform to the tile in shared memory (first
+// pass of a float sort), so that the ranking loop reads ordered keys.
+template <typename K, int BLOCK>
+__device__ __forceinline__ void order_tile_in_place(K* s_keys, uint32_t tile_n) {
+  for (uint32_t i = threadIdx.x; i < tile_n; i += BLOCK) s_keys[i] = to_ordered(s_keys[i], true);
+}
+
+// One onesweep tile ranked by warp multisplit: warp w owns the contiguous
+// run [w * 32 * ITEMS, (w + 1) * 32 * ITEMS) of the tile, lane l its items
 // j * 32 + l; for each item the lanes holding the same digit are found with
 // match_digit8, the lowest of them bumps the warp's counter for that digit
 // and every lane takes counter + peers below it, so ranks follow tile order.
 // Per-bin warp counters are scanned across warps into tile offsets; keys are
 // staged in shared memory at their in-tile sorted position and written out
-// as in onesweep_tile.
+// in bin-contiguous runs after the look-back.
+//
+// Called by all BLOCK threads after a barrier that ends every earlier use of
+// `sm`; the tile's bulk copy (if the pass bulk-copies) was started on `bar`
+// with tile_issue_load, and `parity` is the phase it completes (flipped here).
 template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, typename S>
-__device__ __forceinline__ void onesweep_tile_multisplit(const TileJob<K, S>& job, unsigned char* smem,
-                                                         uint64_t* s_bar, uint32_t& parity) {
-  using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
+__device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, const TileSmem<K, S>& sm,
+                                                      uint64_t* s_bar, uint32_t& parity) {
   using SW = StatusWord<S>;
-  constexpr int TILE = G::kTile;
-  constexpr int WARPS = G::kWarps;
+  constexpr int TILE = BLOCK * ITEMS;
+  constexpr int WARPS = BLOCK / 32;
   constexpr uint32_t FULL = 0xFFFFFFFFu;
-  static_assert((size_t)WARPS * kRadix <= (size_t)kNibbleBins * G::kCntRow, "warp counters fit the counter area");
-  K* s_keys = reinterpret_cast<K*>(smem + G::kKeysOff);
-  uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + G::kValsOff);
-  uint32_t* s_wh = reinterpret_cast<uint32_t*>(smem + G::kCntOff);  // [WARPS][256]
-  S* s_base = reinterpret_cast<S*>(smem + G::kBinBaseOff);
-  uint32_t* s_tstart = reinterpret_cast<uint32_t*>(smem + G::kBinStartOff);
-  uint32_t* s_tcount = reinterpret_cast<uint32_t*>(smem + G::kBinEndOff);
-  uint32_t* s_abort = reinterpret_cast<uint32_t*>(smem + G::kAbortOff);
+  K* s_keys = sm.keys;
+  uint32_t* s_vals = sm.vals;
+  uint32_t* s_wh = sm.wh;
+  S* s_base = sm.base;
+  uint32_t* s_tstart = sm.tstart;
+  uint32_t* s_tcount = sm.tcount;
+  uint32_t* s_abort = sm.abort;
 
   const K* in = job.in;
   K* out = job.out;
@@ -467,24 +530,15 @@ __device__ __forceinline__ void onesweep_tile_multisplit(const TileJob<K, S>& jo
   const uint32_t tile_n = (uint32_t)min((size_t)TILE, job.n - tile_base);
   const bool full = tile_n == (uint32_t)TILE;
   if (tid == 0) *s_abort = 0;
-  for (uint32_t i = tid; i < (uint32_t)(WARPS * kRadix); i += BLOCK) s_wh[i] = 0;
+  for (uint32_t i = tid; i < (uint32_t)(kMatchWords * WARPS * kRadix); i += BLOCK) s_wh[i] = 0;
 
-  // tile -> shared memory (bulk copy; plain loads for the ragged end)
-  const bool tma_ok = ((reinterpret_cast<uintptr_t>(in) & 15u) == 0) &&
-                      (!HAS_VALS || (reinterpret_cast<uintptr_t>(vin) & 15u) == 0);
+  // the ragged end (or, without bulk copies, everything) with plain loads
+  const bool tma_ok = tile_tma_ok<K, HAS_VALS>(job);
   uint32_t loaded = 0;
   if (tma_ok) {
-    const uint32_t kbulk = (tile_n * (uint32_t)sizeof(K)) & ~15u;
-    const uint32_t vbulk = HAS_VALS ? ((tile_n * 4u) & ~15u) : 0u;
-    if (tid == 0) {
-      fence_proxy_async();
-      mbar_arrive_expect_tx(s_bar, kbulk + vbulk);
-      if (kbulk) bulk_load_g2s(s_keys, in + tile_base, kbulk, s_bar);
-      if (HAS_VALS && vbulk) bulk_load_g2s(s_vals, vin + tile_base, vbulk, s_bar);
-    }
-    loaded = kbulk / (uint32_t)sizeof(K);
+    loaded = ((tile_n * (uint32_t)sizeof(K)) & ~15u) / (uint32_t)sizeof(K);
     if (HAS_VALS)
-      for (uint32_t i = vbulk / 4u + tid; i < tile_n; i += BLOCK) s_vals[i] = vin[tile_base + i];
+      for (uint32_t i = ((tile_n * 4u) & ~15u) / 4u + tid; i < tile_n; i += BLOCK) s_vals[i] = vin[tile_base + i];
   } else if (HAS_VALS) {
     for (uint32_t i = tid; i < tile_n; i += BLOCK) s_vals[i] = vin[tile_base + i];
   }
@@ -494,6 +548,10 @@ __device__ __forceinline__ void onesweep_tile_multisplit(const TileJob<K, S>& jo
     parity ^= 1u;
   }
   __syncthreads();
+  if (job.tin) {
+    order_tile_in_place<K, BLOCK>(s_keys, tile_n);
+    __syncthreads();
+  }
 
   // rank within the warp
   const uint32_t dsel = 0x4440u | ((shift >> 3) & 3u);
@@ -506,13 +564,27 @@ __device__ __forceinline__ void onesweep_tile_multisplit(const TileJob<K, S>& jo
   uint32_t rk[(ITEMS + 1) / 2];  // in-warp ranks (< 32 * ITEMS), two 16-bit halves per word
 #pragma unroll
   for (int q = 0; q < (ITEMS + 1) / 2; ++q) rk[q] = 0;
-#pragma unroll
-  for (int j = 0; j < ITEMS; ++j) {
+  auto rank_item = [&](auto jc) {
+    constexpr int j = decltype(jc)::value;
     const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
     const bool valid = full || idx < tile_n;
-    k[j] = valid ? to_ordered(s_keys[idx], job.tin) : (K)0;
+    k[j] = valid ? s_keys[idx] : (K)0;
     if (HAS_VALS) v[j] = valid ? s_vals[idx] : 0u;
     const uint32_t d = digit8(k[j], dsel, dupper);
+#if PA_MATCH_ATOMIC_OR
+    uint32_t* mw = s_wh + WARPS * kRadix + warp * kRadix + d;
+    if (valid) atomicOr(mw, 1u << lane);
+    __syncwarp();
+    const uint32_t peers = valid ? *mw : 0u;
+    __syncwarp();
+    const uint32_t leader = 31u - __clz(peers | (valid ? 0u : 1u));
+    uint32_t base = 0;
+    if (lane == leader && valid) {
+      base = wh[d];
+      wh[d] = base + __popc(peers);
+      *mw = 0u;
+    }
+#else
     uint32_t peers = match_digit8(d);
     if (!full) {
       const uint32_t vm = __ballot_sync(FULL, valid);
@@ -524,10 +596,12 @@ __device__ __forceinline__ void onesweep_tile_multisplit(const TileJob<K, S>& jo
       base = wh[d];
       wh[d] = base + __popc(peers);
     }
+#endif
     base = __shfl_sync(FULL, base, leader);
     rk[j / 2] |= (base + __popc(peers & lt)) << (16 * (j % 2));
     __syncwarp();
-  }
+  };
+  static_for<ITEMS>(rank_item);
   __syncthreads();
 
   // per bin: exclusive scan over warps, tile count, publish
@@ -607,10 +681,15 @@ __device__ __forceinline__ void onesweep_tile_multisplit(const TileJob<K, S>& jo
           if (flag == 2u) done = true;
         }
         t -= used;
-        if (!done && used == 0 && ++spins > kSpinLimit) {
-          raise_error(job.err, DEVERR_LOOKBACK_TIMEOUT);
-          *s_abort = 1;
-          break;
+        if (!done && used == 0) {
+          ++spins;
+          // give up once the limit is reached, or early once another tile
+          // has already reported a failure (its successors would wait in vain)
+          if (spins > kSpinLimit || ((spins & 1023u) == 0 && ld_relaxed_gpu(job.err) != 0)) {
+            raise_error(job.err, DEVERR_LOOKBACK_TIMEOUT);
+            *s_abort = 1;
+            break;
+          }
         }
       }
       S* st = job.status + (size_t)tile * kRadix + tid;
@@ -650,6 +729,27 @@ __device__ __forceinline__ void onesweep_tile_multisplit(const TileJob<K, S>& jo
     scatter([](K x) { return from_ordered(x, true); });
   else
     scatter([](K x) { return x; });
+}
+
+// One multisplit tile in the Geometry layout (one tile buffer at offset 0):
+// starts its bulk copy and runs the body.  Used where one CTA handles one
+// tile at a time (the batched kernel).
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, typename S>
+__device__ __forceinline__ void onesweep_tile_multisplit(const TileJob<K, S>& job, unsigned char* smem,
+                                                         uint64_t* s_bar, uint32_t& parity) {
+  using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
+  static_assert((size_t)kMatchWords * G::kWarps * kRadix <= (size_t)kNibbleBins * G::kCntRow,
+                "warp counters (and match words) fit the counter area");
+  TileSmem<K, S> sm;
+  sm.keys = reinterpret_cast<K*>(smem + G::kKeysOff);
+  sm.vals = reinterpret_cast<uint32_t*>(smem + G::kValsOff);
+  sm.wh = reinterpret_cast<uint32_t*>(smem + G::kCntOff);
+  sm.base = reinterpret_cast<S*>(smem + G::kBinBaseOff);
+  sm.tstart = reinterpret_cast<uint32_t*>(smem + G::kBinStartOff);
+  sm.tcount = reinterpret_cast<uint32_t*>(smem + G::kBinEndOff);
+  sm.abort = reinterpret_cast<uint32_t*>(smem + G::kAbortOff);
+  if (threadIdx.x == 0) tile_issue_load<K, HAS_VALS, G::kTile>(job, job.tile, sm.keys, sm.vals, s_bar);
+  onesweep_tile_ms_body<K, HAS_VALS, BLOCK, ITEMS, S>(job, sm, s_bar, parity);
 }
 
 }  // namespace os

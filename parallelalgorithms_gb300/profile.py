@@ -19,7 +19,7 @@ import numpy as np
 def main() -> None:
     p = argparse.ArgumentParser()
     p.add_argument("--op", default="sort_u32",
-                   choices=["sort_u32", "sort_kv_u64", "sort_f32", "hist_u32", "select_u32", "sum_u32"])
+                   choices=["sort_u32", "sort_u64", "sort_kv_u64", "sort_f32", "hist_u32", "select_u32", "sum_u32"])
     p.add_argument("--n", type=int, default=50_000_000)
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--dist", default="uniform", choices=["uniform", "presorted", "constant"])
@@ -32,7 +32,7 @@ def main() -> None:
     lib = _native.lib()
     P = ctypes.c_void_p
     n = a.n
-    if a.op == "sort_kv_u64":
+    if a.op in ("sort_kv_u64", "sort_u64"):
         keys = workloads.uniform_u64(n)
     elif a.op == "sort_f32":
         keys = workloads.normal_specials_f32(n).view(np.uint32)
@@ -58,6 +58,8 @@ def main() -> None:
             _native.call("pa_sort_u32", P(k.data_ptr()), P(t.data_ptr()), n, o)
         elif a.op == "sort_f32":
             _native.call("pa_sort_f32", P(k.data_ptr()), P(t.data_ptr()), n, o)
+        elif a.op == "sort_u64":
+            _native.call("pa_sort_u64", P(k.data_ptr()), P(t.data_ptr()), n, o)
         elif a.op == "sort_kv_u64":
             _native.call("pa_sort_kv_u64", P(k.data_ptr()), P(v.data_ptr()), P(t.data_ptr()), P(tv.data_ptr()), n, o)
         elif a.op == "hist_u32":
