@@ -337,7 +337,7 @@ int sum_impl(const void* a, size_t n, int kb, uint64_t* out, const pa_opts* opts
   layout(r);
   if (!in_dev && n) PA_CUDA(cudaMemcpyAsync(const_cast<void*>(d_in), a, n * kb, cudaMemcpyHostToDevice, stream));
   PA_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream));
-  PA_CUDA(launch_sum(d_in, n, kb, partials, ticket, d_out, stream));
+  PA_CUDA(launch_sum(d_in, n, kb, partials, ticket, d_out, ws->err, stream));
   if (!out_dev) PA_CUDA(cudaMemcpyAsync(out, d_out, sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
   return finish(ws, stream, opts && opts->async_device && in_dev && out_dev);
 }

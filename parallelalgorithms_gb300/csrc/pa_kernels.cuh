@@ -122,10 +122,11 @@ cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32
 
 // ---- sum (pa_sum.cu) -------------------------------------------------------
 // out = sum of keys[0, n) modulo 2^64.  partials holds sum_partials_needed()
-// words and ticket one zeroed word.
+// words and ticket one zeroed word; a bulk-copy wait that gives up raises a
+// bit in *err.
 size_t sum_partials_needed();
 cudaError_t launch_sum(const void* keys, size_t n, int key_bytes, unsigned long long* partials, uint32_t* ticket,
-                       unsigned long long* out, cudaStream_t stream);
+                       unsigned long long* out, uint32_t* err, cudaStream_t stream);
 
 // ---- select (pa_select.cu) -------------------------------------------------
 struct SelectState;

@@ -218,6 +218,22 @@ def test_unaligned_device_buffers(pa, port, torch_cuda):
     np.testing.assert_array_equal(from_dev(view, np.uint32), want)
 
 
+def test_select_unaligned_device_buffers(pa, port, torch_cuda):
+    # a device view that does not start on 16 bytes: its head and tail are read
+    # with plain loads, the rest with 16-byte vectors
+    for n in (5, 100003, 1 << 20):
+        a = u32_inputs(n + 3)["uniform"]
+        base = to_dev(torch_cuda, a)
+        for off in (1, 2, 3):
+            m = n + 3 - off
+            view = base[off:]
+            for k in sorted({0, m // 2, m - 1}):
+                assert pa.select(view, k) == port.select(a[off:], k), (n, off, k)
+        a64 = np.arange(n + 1, dtype=np.uint64)[::-1].copy()
+        v64 = torch_cuda.from_numpy(a64.view(np.int64)).cuda()[1:]
+        assert pa.select(v64, n // 3) == port.select(a64[1:], n // 3)
+
+
 def test_repeated_calls_reuse_workspace(pa, port):
     for n in (100003, 5, 1 << 20, 100003, 3):
         a = u32_inputs(n)["uniform"]
