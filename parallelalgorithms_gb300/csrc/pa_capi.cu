@@ -10,6 +10,7 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -67,12 +68,19 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 constexpr int kMaxEvents = 16;
 
+constexpr int kPipeChunks = 8;   // host-buffer sort: copy-in chunks
+constexpr int kPipeGroups = 8;   // host-buffer sort: bucket groups sorted and copied out in turn
+
 struct Workspace {
   char* dev = nullptr;
   size_t dev_cap = 0;
   uint32_t* err = nullptr;       // device error word, zero between calls
   uint32_t* err_host = nullptr;  // pinned mirror for reading it back
   cudaEvent_t ev[kMaxEvents] = {};  // phase timing (created on first use)
+  // pipelined host-buffer sort (created on first use)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t pipe_ev[kPipeChunks + kPipeGroups + 2] = {};
+  unsigned long long* pipe_host = nullptr;  // pinned: per-chunk counts, per-group pieces
 };
 
 std::mutex g_mu;
@@ -163,6 +171,158 @@ int finish(Workspace* ws, cudaStream_t stream, bool async_ok) {
 // ---------------------------------------------------------------------------
 // Sort
 // ---------------------------------------------------------------------------
+// Host-buffer sorts of many keys hide most of the sort behind the host-link
+// copies (same result, bit for bit):
+//   1. the keys are copied in by chunks on a copy stream; as each chunk
+//      arrives, the call's stream counts its top digit and runs one onesweep
+//      pass on it, which splits the chunk into 256 buckets in key order
+//      (stable) in the scratch array;
+//   2. consecutive buckets are cut into groups of about n / kPipeGroups keys;
+//      a group's keys are gathered from every chunk in chunk order (so keys
+//      of one bucket keep their input order), sorted on their own by the
+//      plain sort, and copied out on the copy stream while the next group
+//      is gathered and sorted.
+// Returns PA_OK after enqueueing everything; the caller's stream waits for
+// the last copy.
+constexpr size_t kPipeMinKeys = (size_t)1 << 24;
+
+// Groups per pipelined sort (at most kPipeGroups; PA_HOST_PIPELINE_GROUPS
+// overrides the default for tuning).
+int pipe_groups() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("PA_HOST_PIPELINE_GROUPS");
+    v = e ? std::atoi(e) : kPipeGroups;
+    if (v < 1 || v > kPipeGroups) v = kPipeGroups;
+  }
+  return v;
+}
+
+bool pipeline_enabled() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("PA_HOST_PIPELINE");
+    v = (e && std::strcmp(e, "0") == 0) ? 0 : 1;
+  }
+  return v == 1;
+}
+
+int pipelined_host_sort(Workspace* ws, cudaStream_t stream, void* keys, size_t n, int kb) {
+  static_assert(kPipeChunks <= 16, "a group gathers at most 16 pieces");
+  constexpr size_t kHostWords = (size_t)kPipeChunks * 256 + (size_t)kPipeGroups * kPipeChunks * 2;
+  if (!ws->copy_stream) PA_CUDA(cudaStreamCreateWithFlags(&ws->copy_stream, cudaStreamNonBlocking));
+  for (auto& e : ws->pipe_ev)
+    if (!e) PA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  if (!ws->pipe_host) PA_CUDA(cudaMallocHost(&ws->pipe_host, kHostWords * 8));
+  const uint32_t top_shift = 8u * (uint32_t)kb - 8u;
+  const size_t chunk = ((n + kPipeChunks - 1) / kPipeChunks + 3) & ~(size_t)3;
+  const size_t ctiles = ceil_div(chunk, onesweep_tile_keys(kb, false));
+  const size_t sb = onesweep_status_bytes(chunk);
+  char *d_keys = nullptr, *d_tmp = nullptr, *d_gs = nullptr, *status = nullptr, *gscratch = nullptr;
+  unsigned long long *counts = nullptr, *bin_start = nullptr, *pieces = nullptr;
+  uint32_t* tile_ctr = nullptr;
+  SortCtrl* ctrl = nullptr;
+  auto layout = [&](Carve& c) {
+    d_keys = c.take<char>(n * kb);  // input chunks; later the gathered groups
+    d_tmp = c.take<char>(n * kb);   // chunks split into buckets
+    d_gs = c.take<char>(n * kb);    // the group sorts' scratch
+    counts = c.take<unsigned long long>((size_t)kPipeChunks * 256);
+    tile_ctr = c.take<uint32_t>(kPipeChunks);
+    status = c.take<char>((size_t)kPipeChunks * ctiles * 256 * sb);
+    bin_start = c.take<unsigned long long>((size_t)kPipeChunks * 256);
+    ctrl = c.take<SortCtrl>(kPipeChunks);
+    pieces = c.take<unsigned long long>((size_t)kPipeGroups * kPipeChunks * 2);
+    gscratch = c.take<char>(sort_scratch_bytes(n, kb, false));
+  };
+  Carve m{nullptr};
+  layout(m);
+  if (int rc = ensure_dev(ws, stream, m.off)) return rc;
+  Carve r{ws->dev};
+  layout(r);
+  const size_t zero_bytes = (size_t)(status + (size_t)kPipeChunks * ctiles * 256 * sb - reinterpret_cast<char*>(counts));
+  cudaEvent_t* ev = ws->pipe_ev;
+  cudaStream_t cs = ws->copy_stream;
+  char* h = static_cast<char*>(keys);
+
+  // 1. chunked copy-in; each arrived chunk is counted and split by its top digit
+  PA_CUDA(cudaMemsetAsync(counts, 0, zero_bytes, stream));
+  PA_CUDA(cudaEventRecord(ev[0], stream));  // earlier work on this workspace is ordered before the copies
+  PA_CUDA(cudaStreamWaitEvent(cs, ev[0], 0));
+  size_t clo[kPipeChunks + 1];
+  int nc = 0;
+  for (int c = 0; c < kPipeChunks; ++c) {
+    const size_t lo = std::min(n, (size_t)c * chunk), hi = std::min(n, lo + chunk);
+    if (lo == hi) break;
+    clo[nc++] = lo;
+    PA_CUDA(cudaMemcpyAsync(d_keys + lo * kb, h + lo * kb, (hi - lo) * kb, cudaMemcpyHostToDevice, cs));
+    PA_CUDA(cudaEventRecord(ev[1 + c], cs));
+    PA_CUDA(cudaStreamWaitEvent(stream, ev[1 + c], 0));
+    unsigned long long* cnt = counts + (size_t)c * 256;
+    unsigned long long* bs = bin_start + (size_t)c * 256;
+    PA_CUDA(launch_digit_counts(d_keys + lo * kb, hi - lo, kb, 1, 8, top_shift, 0, false, cnt, stream));
+    PA_CUDA(launch_scan_digits(cnt, 1, 8, hi - lo, false, false, bs, &ctrl[c], stream));
+    OnesweepArgs a{};
+    a.keys_a = d_keys + lo * kb;
+    a.keys_b = d_tmp + lo * kb;
+    a.n = hi - lo;
+    a.shift = top_shift;
+    a.pass = 0;
+    a.bin_start = bs;
+    a.status = status + (size_t)c * ctiles * 256 * sb;
+    a.tile_counter = tile_ctr + c;
+    a.ctrl = &ctrl[c];
+    a.err = ws->err;
+    PA_CUDA(launch_onesweep_pass(a, kb, false, stream));
+  }
+  clo[nc] = n;
+  unsigned long long* hc = ws->pipe_host;  // [chunks][256] counts
+  PA_CUDA(cudaMemcpyAsync(hc, counts, (size_t)nc * 256 * 8, cudaMemcpyDeviceToHost, stream));
+  PA_CUDA(cudaStreamSynchronize(stream));
+
+  // 2. groups of whole buckets; each group's pieces, one per chunk
+  unsigned long long total[257] = {};
+  for (int b = 0; b < 256; ++b)
+    for (int c = 0; c < nc; ++c) total[b + 1] += hc[(size_t)c * 256 + b];
+  for (int b = 0; b < 256; ++b) total[b + 1] += total[b];  // total[b] = keys in buckets < b
+  if (total[256] != n) return set_error(PA_ERR_CUDA, "top-digit counts add up to %llu, not %zu", total[256], n);
+  int gb[kPipeGroups + 1];  // group g = buckets [gb[g], gb[g + 1])
+  int ng = 0;
+  gb[0] = 0;
+  const int want_groups = pipe_groups();
+  const size_t share = (n + want_groups - 1) / want_groups;
+  for (int b = 1; b < 256 && ng < want_groups - 1; ++b)
+    if (total[b] - total[gb[ng]] >= share && total[b] < n) gb[++ng] = b;
+  gb[++ng] = 256;
+  unsigned long long* hp = hc + (size_t)kPipeChunks * 256;  // [groups][chunks] (offset, count)
+  for (int c = 0; c < nc; ++c) {
+    unsigned long long start = 0;  // the chunk's bucket starts, walked group by group
+    int b = 0;
+    for (int g = 0; g < ng; ++g) {
+      const unsigned long long gstart = start;
+      for (; b < gb[g + 1]; ++b) start += hc[(size_t)c * 256 + b];
+      hp[((size_t)g * kPipeChunks + c) * 2] = clo[c] + gstart;
+      hp[((size_t)g * kPipeChunks + c) * 2 + 1] = start - gstart;
+    }
+  }
+  PA_CUDA(cudaMemcpyAsync(pieces, hp, (size_t)ng * kPipeChunks * 2 * 8, cudaMemcpyHostToDevice, stream));
+
+  // 3. per group: gather, sort, copy out while the next group runs
+  for (int g = 0; g < ng; ++g) {
+    const size_t lo = (size_t)total[gb[g]], len = (size_t)(total[gb[g + 1]] - total[gb[g]]);
+    if (len == 0) continue;
+    PA_CUDA(launch_gather_pieces(d_tmp, d_keys + lo * kb, pieces + (size_t)g * kPipeChunks * 2, nc, len, kb, stream));
+    SortScratch sc{};
+    sort_scratch_layout(gscratch, len, kb, false, &sc);
+    PA_CUDA(enqueue_sort(sc, d_keys + lo * kb, d_gs + lo * kb, nullptr, nullptr, len, kb, false, ws->err, stream));
+    PA_CUDA(cudaEventRecord(ev[1 + kPipeChunks + g], stream));
+    PA_CUDA(cudaStreamWaitEvent(cs, ev[1 + kPipeChunks + g], 0));
+    PA_CUDA(cudaMemcpyAsync(h + lo * kb, d_keys + lo * kb, len * kb, cudaMemcpyDeviceToHost, cs));
+  }
+  PA_CUDA(cudaEventRecord(ev[kPipeChunks + kPipeGroups + 1], cs));
+  PA_CUDA(cudaStreamWaitEvent(stream, ev[kPipeChunks + kPipeGroups + 1], 0));
+  return PA_OK;
+}
+
 // phase_ms (optional, phase_cap entries): device time of each kernel of the
 // sort from CUDA events recorded between launches on the call's stream:
 // [0] digit histogram, [1] scan, [2 + p] digit pass p, [2 + passes] final
@@ -182,6 +342,17 @@ int sort_impl(void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t 
   const bool has_vals = vals != nullptr;
   const bool keys_dev = is_device_ptr(keys);
   const bool tmp_dev = is_device_ptr(tmp);
+  if (!keys_dev && !has_vals && !is_float && !(phase_ms && phase_cap > 0) && n >= kPipeMinKeys &&
+      pipeline_enabled()) {
+    if (int rc = pipelined_host_sort(ws, stream, keys, n, kb)) {
+      // nothing may still copy into the caller's buffer after the call returns
+      if (ws->copy_stream) cudaStreamSynchronize(ws->copy_stream);
+      cudaStreamSynchronize(stream);
+      cudaGetLastError();
+      return rc;
+    }
+    return finish(ws, stream, false);
+  }
   const bool vals_dev = has_vals && is_device_ptr(vals);
   const bool tvals_dev = has_vals && is_device_ptr(tmp_vals);
   void *d_keys = nullptr, *d_tmp = nullptr;

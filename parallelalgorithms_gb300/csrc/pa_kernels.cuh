@@ -92,6 +92,12 @@ size_t onesweep_tile_keys(int key_bytes, bool has_vals);
 size_t onesweep_status_bytes(size_t n);
 cudaError_t launch_onesweep_pass(const OnesweepArgs& a, int key_bytes, bool has_vals, cudaStream_t stream);
 
+// dst[0, total) = the concatenation of `npieces` runs of src, piece i being
+// src[pieces[2i], pieces[2i] + pieces[2i + 1]) (element offsets and counts;
+// npieces <= 16).  key_bytes 4 or 8.
+cudaError_t launch_gather_pieces(const void* src, void* dst, const unsigned long long* pieces, int npieces,
+                                 size_t total, int key_bytes, cudaStream_t stream);
+
 // Copies the result back into the caller's buffers when the executed passes
 // left it in the scratch buffers (device-side decision from SortCtrl).
 cudaError_t launch_final_copy(void* keys_a, const void* keys_b, uint32_t* vals_a, const uint32_t* vals_b,

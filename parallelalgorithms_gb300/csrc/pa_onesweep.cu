@@ -94,6 +94,38 @@ __global__ void final_copy_kernel(K* keys_a, const K* keys_b, uint32_t* vals_a, 
   }
 }
 
+// One grid row per piece: the piece's elements go to their place in dst with
+// 16-byte vector stores (the loads are plain and coalesced: a warp reads
+// consecutive elements); the few elements before dst's first 16-byte
+// boundary and after its last one are copied singly.
+template <typename K>
+__global__ void gather_pieces_kernel(const K* __restrict__ src, K* __restrict__ dst,
+                                     const unsigned long long* __restrict__ pieces, int npieces) {
+  constexpr uint32_t V = 16 / sizeof(K);
+  const int p = blockIdx.y;
+  unsigned long long d0 = 0;  // where the piece starts in dst
+  for (int q = 0; q < p; ++q) d0 += pieces[2 * q + 1];
+  const K* s = src + pieces[2 * p];
+  const size_t len = (size_t)pieces[2 * p + 1];
+  K* d = dst + d0;
+  size_t head = ((16u - (reinterpret_cast<uintptr_t>(d) & 15u)) & 15u) / sizeof(K);
+  if (head > len) head = len;
+  const size_t nvec = (len - head) / V;
+  const size_t tail = head + nvec * V;
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  if (tid < head) d[tid] = s[tid];
+  if (tid < len - tail) d[tail + tid] = s[tail + tid];
+  uint4* dv = reinterpret_cast<uint4*>(d + head);
+  for (size_t j = tid; j < nvec; j += stride) {
+    const K* e = s + head + j * V;
+    K v[V];
+#pragma unroll
+    for (uint32_t k = 0; k < V; ++k) v[k] = e[k];
+    dv[j] = *reinterpret_cast<const uint4*>(v);
+  }
+}
+
 // Tile geometries.  Each is (threads, keys per thread, CTAs per SM the
 // register budget is cut for).  The active one per (key type, payload) is
 // the first entry unless PA_ONESWEEP_GEOMETRY selects another (tuning).
@@ -208,6 +240,28 @@ cudaError_t launch_onesweep_pass(const OnesweepArgs& a, int key_bytes, bool has_
   if (a.n == 0) return cudaSuccess;
   if (key_bytes == 4) return has_vals ? launch_kv<uint32_t, true>(a, stream) : launch_kv<uint32_t, false>(a, stream);
   return has_vals ? launch_kv<unsigned long long, true>(a, stream) : launch_kv<unsigned long long, false>(a, stream);
+}
+
+cudaError_t launch_gather_pieces(const void* src, void* dst, const unsigned long long* pieces, int npieces,
+                                 size_t total, int key_bytes, cudaStream_t stream) {
+  if (total == 0) return cudaSuccess;
+  if (npieces < 1 || npieces > 16) return cudaErrorInvalidValue;
+  const int block = 256;
+  // each piece gets about total / npieces elements; a CTA moves 16 vectors per thread
+  const size_t per_piece = ceil_div(total, (size_t)npieces);
+  const size_t vec = 16 / (size_t)key_bytes;
+  const unsigned gx = (unsigned)max((size_t)1, min(ceil_div(per_piece, (size_t)block * vec * 16),
+                                                   (size_t)device_info().sm_count * 2));
+  const dim3 grid(gx, (unsigned)npieces);
+  if (key_bytes == 4)
+    gather_pieces_kernel<uint32_t><<<grid, block, 0, stream>>>(static_cast<const uint32_t*>(src),
+                                                               static_cast<uint32_t*>(dst), pieces, npieces);
+  else if (key_bytes == 8)
+    gather_pieces_kernel<unsigned long long><<<grid, block, 0, stream>>>(
+        static_cast<const unsigned long long*>(src), static_cast<unsigned long long*>(dst), pieces, npieces);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_final_copy(void* keys_a, const void* keys_b, uint32_t* vals_a, const uint32_t* vals_b,
