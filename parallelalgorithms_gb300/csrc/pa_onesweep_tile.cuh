@@ -483,7 +483,16 @@ __device__ __forceinline__ void tile_issue_load(const TileJob<K, S>& job, uint32
 #ifndef PA_MATCH_ATOMIC_OR
 #define PA_MATCH_ATOMIC_OR 0
 #endif
-constexpr int kMatchWords = PA_MATCH_ATOMIC_OR ? 2 : 1;  // [warps][256] word arrays in TileSmem::wh
+//   PA_MATCH_MIX = m > 0: items j with j % m == 0 find their peers through
+//     shared memory (as PA_MATCH_ATOMIC_OR), the others with ballots, so the
+//     integer pipe (ballots) and the shared-memory pipe (atomic OR, read
+//     back, clear) share the matching work.  Default 3: measured fastest on
+//     GB300 (100M u32 sort 1.78 ms against 1.86 ms all-ballot; 2 and 4-6 in
+//     between, and all-atomic-OR is slower on skewed keys).  0 = ballots only.
+#ifndef PA_MATCH_MIX
+#define PA_MATCH_MIX 3
+#endif
+constexpr int kMatchWords = (PA_MATCH_ATOMIC_OR || PA_MATCH_MIX) ? 2 : 1;  // [warps][256] word arrays in TileSmem::wh
 
 // Applies the float order transform to the tile in shared memory (first
 // pass of a float sort), so that the ranking loop reads ordered keys.
@@ -494,9 +503,11 @@ __device__ __forceinline__ void order_tile_in_place(K* s_keys, uint32_t tile_n) 
 
 // One onesweep tile ranked by warp multisplit: warp w owns the contiguous
 // run [w * 32 * ITEMS, (w + 1) * 32 * ITEMS) of the tile, lane l its items
-// j * 32 + l; for each item the lanes holding the same digit are found with
-// match_digit8, the lowest of them bumps the warp's counter for that digit
-// and every lane takes counter + peers below it, so ranks follow tile order.
+// j * 32 + l; for each item the lanes holding the same digit (its peers) are
+// found with the eight ballots of match_digit8, or for every PA_MATCH_MIX-th
+// item by an atomic OR of the lane bit into the warp's shared word for the
+// digit; one lane of the group bumps the warp's counter for that digit and
+// every lane takes counter + peers below it, so ranks follow tile order.
 // Per-bin warp counters are scanned across warps into tile offsets; keys are
 // staged in shared memory at their in-tile sorted position and written out
 // in bin-contiguous runs after the look-back.
@@ -571,32 +582,36 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
     k[j] = valid ? s_keys[idx] : (K)0;
     if (HAS_VALS) v[j] = valid ? s_vals[idx] : 0u;
     const uint32_t d = digit8(k[j], dsel, dupper);
-#if PA_MATCH_ATOMIC_OR
-    uint32_t* mw = s_wh + WARPS * kRadix + warp * kRadix + d;
-    if (valid) atomicOr(mw, 1u << lane);
-    __syncwarp();
-    const uint32_t peers = valid ? *mw : 0u;
-    __syncwarp();
-    const uint32_t leader = 31u - __clz(peers | (valid ? 0u : 1u));
-    uint32_t base = 0;
-    if (lane == leader && valid) {
-      base = wh[d];
-      wh[d] = base + __popc(peers);
-      *mw = 0u;
-    }
+#if PA_MATCH_ATOMIC_OR || PA_MATCH_MIX
+    constexpr bool kSmemMatch = PA_MATCH_ATOMIC_OR || (PA_MATCH_MIX > 0 && j % (PA_MATCH_MIX > 0 ? PA_MATCH_MIX : 1) == 0);
 #else
-    uint32_t peers = match_digit8(d);
-    if (!full) {
-      const uint32_t vm = __ballot_sync(FULL, valid);
-      peers &= valid ? vm : ~vm;
-    }
-    const uint32_t leader = __ffs(peers) - 1;
-    uint32_t base = 0;
-    if (lane == leader && valid) {
-      base = wh[d];
-      wh[d] = base + __popc(peers);
-    }
+    constexpr bool kSmemMatch = false;
 #endif
+    uint32_t peers, leader, base = 0;
+    if constexpr (kSmemMatch) {
+      uint32_t* mw = s_wh + WARPS * kRadix + warp * kRadix + d;
+      if (valid) atomicOr(mw, 1u << lane);
+      __syncwarp();
+      peers = valid ? *mw : 0u;
+      __syncwarp();
+      leader = 31u - __clz(peers | (valid ? 0u : 1u));
+      if (lane == leader && valid) {
+        base = wh[d];
+        wh[d] = base + __popc(peers);
+        *mw = 0u;
+      }
+    } else {
+      peers = match_digit8(d);
+      if (!full) {
+        const uint32_t vm = __ballot_sync(FULL, valid);
+        peers &= valid ? vm : ~vm;
+      }
+      leader = __ffs(peers) - 1;
+      if (lane == leader && valid) {
+        base = wh[d];
+        wh[d] = base + __popc(peers);
+      }
+    }
     base = __shfl_sync(FULL, base, leader);
     rk[j / 2] |= (base + __popc(peers & lt)) << (16 * (j % 2));
     __syncwarp();
