@@ -134,7 +134,7 @@ struct GeomChoice {
 };
 constexpr GeomChoice kGeomU32[] = {{384, 16, 3}, {512, 16, 2}, {256, 16, 4}, {1024, 8, 1}, {512, 8, 3}};
 constexpr GeomChoice kGeomU32Kv[] = {{512, 12, 2}, {256, 12, 4}, {512, 8, 3}};
-constexpr GeomChoice kGeomU64[] = {{256, 12, 4}, {512, 12, 2}, {512, 8, 3}};
+constexpr GeomChoice kGeomU64[] = {{512, 12, 2}, {256, 12, 4}, {512, 8, 3}};
 constexpr GeomChoice kGeomU64Kv[] = {{256, 12, 3}, {256, 8, 4}, {512, 8, 2}};
 
 int geometry_index(int count) {
