@@ -606,6 +606,19 @@ def run_extras(pa, lib, _native, workloads, n, stream, peak) -> dict:
                                    "frac": 4 * n / (ms / 1e3) / 1e9 / peak}
         _native.call("pa_stream_check", P(stream.cuda_stream))
         del d
+    # byte counting sort (CountingSortParallel.h:81), 400 MB of uniform bytes:
+    # one histogram read + one fill write = 2 B/byte
+    nb = 4 * n
+    bsrc = torch.randint(0, 256, (nb,), dtype=torch.uint8, device="cuda",
+                         generator=torch.Generator(device="cuda").manual_seed(1241))
+    bw = torch.empty_like(bsrc)
+    ms = _time_device(lambda: _native.call("pa_counting_sort_u8", P(bw.data_ptr()), nb, o), 5, stream,
+                      lambda: bw.copy_(bsrc))
+    ok = bool(torch.all(bw[1:] >= bw[:-1]))
+    out["counting_sort_u8_400MB"] = {"ms": ms, "bytes_per_s_sorted": nb / (ms / 1e3), "bytes_per_key": 2,
+                                     "achieved_gbs": 2 * nb / (ms / 1e3) / 1e9,
+                                     "frac": 2 * nb / (ms / 1e3) / 1e9 / peak, "sorted": ok}
+    del bsrc, bw
     out["batched_segmented_sort_4096_arrays"] = batched_extra(lib, _native, workloads, stream, peak)
     out["serving_c5"] = serving_extra()
     return out

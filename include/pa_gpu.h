@@ -259,6 +259,12 @@ int pa_server_drain(pa_server* server);
 int pa_server_stats(pa_server* server, uint64_t* out, int count);
 int pa_server_destroy(pa_server* server);
 
+/* Byte-array counting sort, in place: replaces counting_sort_parallel(a,
+ * a_size) (CountingSortParallel.h:81-91) and counting_sort_parallel_inner<256>
+ * (:29-79): a one-read byte histogram, then a parallel fill of each value's
+ * range. */
+int pa_counting_sort_u8(uint8_t* a, size_t n, const pa_opts* opts);
+
 /* 256-bin histogram of (key >> shift) & 255 over 64-bit keys (no reference
  * counterpart; the 32-bit form is pa_hist_one_byte_u32). shift < 64. */
 int pa_hist_one_byte_u64(const uint64_t* a, size_t n, unsigned shift, uint64_t* out, const pa_opts* opts);

@@ -50,6 +50,8 @@ class _Port:
         h.pa_oracle_sum_u32.restype = ctypes.c_uint64
         h.pa_oracle_sum_u64.argtypes = [_P, _SZ, _SZ]
         h.pa_oracle_sum_u64.restype = ctypes.c_uint64
+        h.pa_oracle_counting_sort_u8.argtypes = [_P, _SZ, _SZ]
+        h.pa_oracle_partition_radix_u32.argtypes = [_P, _SZ, _P, _SZ]
         self.h = h
 
     def sort(self, keys: np.ndarray, vals: np.ndarray | None = None, digit_bits: int = 8):
@@ -116,6 +118,19 @@ class _Port:
             return int(self.h.pa_oracle_sum_u64(_p(a), l, r))
         return int(self.h.pa_oracle_sum_u32(_p(a), l, r))
 
+    def counting_sort_u8(self, a: np.ndarray, l: int = 0, r: int | None = None) -> np.ndarray:
+        """Sorted copy of a byte array (counting sort of a[l, r))."""
+        c = np.ascontiguousarray(a).copy()
+        self.h.pa_oracle_counting_sort_u8(_p(c), l, c.size if r is None else r)
+        return c
+
+    def partition_radix(self, a: np.ndarray, ks) -> np.ndarray:
+        """PartitionRadix(a, n, k[], kLength) on a copy; ks ascending."""
+        c = np.ascontiguousarray(a, dtype=np.uint32).copy()
+        k = np.ascontiguousarray(ks, dtype=np.uint64)
+        self.h.pa_oracle_partition_radix_u32(_p(c), c.size, _p(k), k.size)
+        return c
+
 
 class _Ref:
     """The reference's own code (compiled unchanged) behind extern "C"."""
@@ -143,6 +158,8 @@ class _Ref:
         h.pa_ref_std_stable_sort_u64.argtypes = [_P, _SZ]
         h.pa_ref_std_stable_sort_f32_bits.argtypes = [_P, _SZ]
         h.pa_ref_std_stable_sort_kv_u64.argtypes = [_P, _P, _SZ]
+        h.pa_ref_counting_sort_par_u8.argtypes = [_P, _SZ]
+        h.pa_ref_partition_radix_u32.argtypes = [_P, _SZ, _P, _SZ]
         self.h = h
 
     def threads(self) -> int:
@@ -210,6 +227,17 @@ class _Ref:
 
     def sum_template_u32(self, a, l=0, r=None) -> int:
         return int(self.h.pa_ref_sum_par_template_u32(_p(a), l, a.size if r is None else r))
+
+    def counting_sort_u8(self, a: np.ndarray) -> np.ndarray:
+        c = np.ascontiguousarray(a).copy()
+        self.h.pa_ref_counting_sort_par_u8(_p(c), c.size)
+        return c
+
+    def partition_radix(self, a: np.ndarray, ks) -> np.ndarray:
+        c = np.ascontiguousarray(a, dtype=np.uint32).copy()
+        k = np.ascontiguousarray(ks, dtype=np.uint64)
+        self.h.pa_ref_partition_radix_u32(_p(c), c.size, _p(k), k.size)
+        return c
 
     def std_stable_sort_u64(self, a):
         self.h.pa_ref_std_stable_sort_u64(_p(a), a.size)

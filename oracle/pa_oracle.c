@@ -322,3 +322,92 @@ uint64_t pa_oracle_sum_u64(const uint64_t* a, size_t l, size_t r) {
   for (size_t i = l; i < r; i++) s += a[i];
   return s;
 }
+
+/* Byte-array counting sort, CountingSortParallel.h:29-79
+ * (counting_sort_parallel_inner): the counts of every byte value over
+ * a[l, r) (HistogramOneByteComponentParallel_3, :34), their exclusive prefix
+ * as each value's start (:56-59), then each value written counts[value]
+ * times from its start (the parallel fill, :65-68). */
+void pa_oracle_counting_sort_u8(uint8_t* a, size_t l, size_t r) {
+  uint64_t counts[256] = {0};
+  for (size_t i = l; i < r; ++i) counts[a[i]]++;
+  size_t at = l;
+  for (unsigned v = 0; v < 256; ++v) {
+    memset(a + at, (int)v, (size_t)counts[v]);
+    at += (size_t)counts[v];
+  }
+}
+
+/* In-place MSD radix partition around the sorted indices k[kstart,
+ * kstart + klen), RadixPartition.h:30-79 (PartitionRadixMsdUIntInner with
+ * 256 bins, 8-bit digits, insertion sort below 48 keys):
+ *   1. count the digit at `shift` over a[start, start + n);
+ *   2. bins start at the exclusive prefix of the counts; each bin's fill
+ *      cursor starts at its start (:42-45);
+ *   3. cycle-leader permutation (:47-58): take the element at the current
+ *      position; while its bin's cursor is not the current position, swap
+ *      it with the element at that cursor and advance the cursor; store it
+ *      and advance its bin's cursor; then move to the cursor of the first
+ *      bin that is not yet full (the comparison uses the bins' starts with
+ *      start[256] = the range start, as the reference does);
+ *   4. with digits left (shift > 0), for every bin holding one or more of
+ *      the k's (walked in order), recurse into it with those k's when it has
+ *      at least 48 keys, else sort it (:59-78). */
+static void partition_inner(uint32_t* a, size_t start, size_t n, int shift, const size_t* k, size_t kstart,
+                            size_t klen) {
+  const size_t last = start + n;
+  size_t count[256];
+  memset(count, 0, sizeof(count));
+  for (size_t i = start; i < last; ++i) count[(a[i] >> shift) & 255u]++;
+  size_t bstart[257], cursor[256];
+  bstart[0] = cursor[0] = start;
+  bstart[256] = start;
+  for (int b = 1; b < 256; ++b) bstart[b] = cursor[b] = bstart[b - 1] + count[b - 1];
+  size_t next = 1;
+  for (size_t cur = start; cur < last;) {
+    uint32_t x = a[cur];
+    unsigned d;
+    while (cursor[d = (x >> shift) & 255u] != cur) {
+      const uint32_t t = a[cursor[d]];
+      a[cursor[d]++] = x;
+      x = t;
+    }
+    a[cur] = x;
+    cursor[d]++;
+    while (cursor[next - 1] == bstart[next]) next++;
+    cur = cursor[next - 1];
+  }
+  if (shift <= 0) return;
+  const int nshift = shift >= 8 ? shift - 8 : 0;
+  size_t ki = kstart;
+  for (int b = 0; b < 256 && ki < kstart + klen; ++b) {
+    if (bstart[b] < cursor[b] && k[ki] >= bstart[b] && k[ki] < cursor[b]) {
+      const size_t first = ki++;
+      size_t cnt = 1;
+      while (ki < kstart + klen && k[ki] >= bstart[b] && k[ki] < cursor[b]) {
+        ++cnt;
+        ++ki;
+      }
+      const size_t m = cursor[b] - bstart[b];
+      if (m >= 48) {
+        partition_inner(a, bstart[b], m, nshift, k, first, cnt);
+      } else {
+        for (size_t i = bstart[b] + 1; i < cursor[b]; ++i) {  /* insertion sort */
+          const uint32_t v = a[i];
+          size_t j = i;
+          while (j > bstart[b] && a[j - 1] > v) {
+            a[j] = a[j - 1];
+            --j;
+          }
+          a[j] = v;
+        }
+      }
+    }
+  }
+}
+
+/* PartitionRadix(a, aLength, k[], kLength), RadixPartition.h:152-162. */
+void pa_oracle_partition_radix_u32(uint32_t* a, size_t n, const size_t* k, size_t klen) {
+  if (n == 0 || klen == 0) return;
+  partition_inner(a, 0, n, 24, k, 0, klen);
+}

@@ -17,6 +17,8 @@
 #include "RadixSelect.h"
 #include "SumParallel.h"
 #include "RadixSortLSD.h"
+#include "CountingSortParallel.h"
+#include "RadixPartition.h"
 
 // RadixSortLSD.h:37-38 declares these (defined in MemoryUsage.cpp); only the
 // memory-adaptive sorts call them, which are not on the path.  Defined here so
@@ -130,6 +132,14 @@ unsigned long long pa_ref_sum_par_u64(unsigned long long* a, size_t l, size_t r)
 long long pa_ref_sum_par_template_u32(unsigned* a, size_t l, size_t r) {
   return ParallelAlgorithms::SumParallel(a, l, r);
 }
+
+// CountingSortParallel.h:81 counting_sort_parallel(a, a_size): byte array
+// sorted by a parallel histogram and a parallel fill.
+void pa_ref_counting_sort_par_u8(unsigned char* a, size_t n) { ParallelAlgorithms::counting_sort_parallel(a, n); }
+
+// RadixPartition.h:152 PartitionRadix(a, aLength, k[], kLength): in-place MSD
+// radix partition around every k (k ascending).
+void pa_ref_partition_radix_u32(unsigned* a, size_t n, size_t* k, size_t klen) { PartitionRadix(a, n, k, klen); }
 
 // Not in the reference: std::stable_sort baselines for the key types the
 // reference has no radix path for (u64, float32 via its bit pattern, and

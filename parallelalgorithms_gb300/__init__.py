@@ -34,6 +34,7 @@ __all__ = [
     "RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase_DeRandomize",
     "HistogramByteComponentsParallel", "HistogramOneByteComponentParallel", "HistogramByteComponentsQCPar",
     "ComputeStartOfBinsPar", "SelectRadix", "SumParallelNonRecursive", "SumParallel",
+    "counting_sort_parallel", "counting_sort_parallel_inner",
     "sort", "select", "sum_u64", "histogram_digit", "PaError", "lib",
 ]
 
@@ -285,3 +286,23 @@ def SumParallel(in_array, l: int, r: int, parallelThreshold: int = 16 * 1024) ->
 def sum_u64(a) -> int:
     """Sum of a whole uint32/uint64 array modulo 2^64."""
     return _sum(a, 0, _info(a)[1])
+
+
+# ---------------------------------------------------------------------------
+# byte counting sort
+# ---------------------------------------------------------------------------
+def counting_sort_parallel_inner(array_to_sort, l: int, r: int, threshold_count: int = 64 * 1024,
+                                 threshold_fill: int = 64 * 1024) -> None:
+    """CountingSortParallel.h:29 counting_sort_parallel_inner<256>(a, l, r):
+    sorts the bytes a[l, r) (r EXCLUSIVE) in place.  The thresholds are
+    accepted and have no effect."""
+    if _kind(_info(array_to_sort)[2]) != "u8":
+        raise TypeError("counting sort takes a uint8 array")
+    n = max(0, r - l)
+    call("pa_counting_sort_u8", _offset(array_to_sort, l, 1), n, _opts(array_to_sort))
+
+
+def counting_sort_parallel(a, a_size: int | None = None) -> None:
+    """CountingSortParallel.h:81 counting_sort_parallel(a, a_size): sorts the
+    bytes a[0, a_size) in place."""
+    counting_sort_parallel_inner(a, 0, _info(a)[1] if a_size is None else a_size)

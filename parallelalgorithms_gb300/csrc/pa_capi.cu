@@ -709,6 +709,35 @@ int pa_hist_u8(const uint8_t* a, size_t n, uint64_t* out, const pa_opts* opts) {
   return hist_impl(a, n, 1, 1, 0, 0, out, opts);
 }
 
+int pa_counting_sort_u8(uint8_t* a, size_t n, const pa_opts* opts) {
+  if (int rc = check_opts(opts)) return rc;
+  if (n == 0) return PA_OK;
+  if (!a) return set_error(PA_ERR_ARG, "a is NULL");
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t stream = stream_of(opts);
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+  const bool dev = is_device_ptr(a);
+  uint8_t* d_a = nullptr;
+  unsigned long long* counts = nullptr;
+  auto layout = [&](Carve& c) {
+    counts = c.take<unsigned long long>(256);
+    d_a = dev ? a : c.take<uint8_t>(n);
+  };
+  Carve m{nullptr};
+  layout(m);
+  if (int rc = ensure_dev(ws, stream, m.off)) return rc;
+  Carve r{ws->dev};
+  layout(r);
+  if (!dev) PA_CUDA(cudaMemcpyAsync(d_a, a, n, cudaMemcpyHostToDevice, stream));
+  PA_CUDA(cudaMemsetAsync(counts, 0, 256 * sizeof(unsigned long long), stream));
+  PA_CUDA(launch_digit_counts(d_a, n, 1, 1, 8, 0, 0, false, counts, stream));
+  PA_CUDA(launch_counting_fill(d_a, n, counts, stream));
+  if (!dev) PA_CUDA(cudaMemcpyAsync(a, d_a, n, cudaMemcpyDeviceToHost, stream));
+  return finish(ws, stream, opts && opts->async_device && dev);
+}
+
 int pa_hist_quanta_u32(const uint32_t* a, size_t l, size_t r, size_t work_quanta, size_t quanta,
                        unsigned which_byte, uint64_t* out, const pa_opts* opts) {
   if (int rc = check_opts(opts)) return rc;

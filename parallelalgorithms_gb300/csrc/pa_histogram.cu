@@ -290,6 +290,88 @@ cudaError_t launch_quanta_start_of_bins(const unsigned long long* counts, size_t
   return cudaGetLastError();
 }
 
+// Byte counting sort's fill (CountingSortParallel.h:48-68): every CTA
+// rebuilds the 256 value starts (exclusive prefix of the counts) in shared
+// memory; each thread writes 16-byte runs of a[i] = the value whose range
+// holds i, walking a per-thread value cursor forward (its positions only
+// grow), with single bytes before the first and after the last 16-byte
+// boundary of the array.
+__global__ void __launch_bounds__(256) counting_fill_kernel(uint8_t* __restrict__ a, size_t n,
+                                                            const unsigned long long* __restrict__ counts) {
+  __shared__ unsigned long long s_start[257];
+  __shared__ unsigned long long s_warp[8];
+  const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+  const unsigned long long c = counts[t];
+  unsigned long long incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= (uint32_t)o) incl += v;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  unsigned long long before = 0;
+  for (uint32_t w = 0; w < warp; ++w) before += s_warp[w];
+  s_start[t] = before + incl - c;
+  if (t == 255) s_start[256] = before + incl;
+  __syncthreads();
+  // value holding position p: the largest v with s_start[v] <= p (empty values skipped)
+  auto value_at = [&](unsigned long long p) {
+    uint32_t lo = 0, hi = 255;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (s_start[mid] <= p) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  };
+  const size_t head = min(n, (size_t)((16u - (reinterpret_cast<uintptr_t>(a) & 15u)) & 15u));
+  const size_t nvec = (n - head) / 16;
+  const size_t tail = head + nvec * 16;
+  const size_t gt = (size_t)blockIdx.x * blockDim.x + t;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  if (gt < head) a[gt] = (uint8_t)value_at(gt);
+  if (gt < n - tail) a[tail + gt] = (uint8_t)value_at(tail + gt);
+  uint4* av = reinterpret_cast<uint4*>(a + head);
+  uint32_t v = 0;
+  bool have = false;
+  for (size_t j = gt; j < nvec; j += stride) {
+    const unsigned long long p0 = head + j * 16;
+    if (!have) {
+      v = value_at(p0);
+      have = true;
+    }
+    while (s_start[v + 1] <= p0) ++v;  // the cursor only moves forward
+    uint32_t w[4];
+    if (s_start[v + 1] >= p0 + 16) {  // the whole run holds one value
+      const uint32_t rep = v * 0x01010101u;
+      w[0] = w[1] = w[2] = w[3] = rep;
+    } else {
+      uint32_t u = v;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        uint32_t word = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const unsigned long long p = p0 + 4 * q + b;
+          while (s_start[u + 1] <= p) ++u;
+          word |= u << (8 * b);
+        }
+        w[q] = word;
+      }
+    }
+    av[j] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+cudaError_t launch_counting_fill(uint8_t* a, size_t n, const unsigned long long* counts, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  const size_t vec = n / 16 + 1;
+  const unsigned grid = (unsigned)min(ceil_div(vec, (size_t)256 * 8), (size_t)device_info().sm_count * 8);
+  counting_fill_kernel<<<grid < 1 ? 1 : grid, 256, 0, stream>>>(a, n, counts);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_scan_digits(const unsigned long long* counts, int passes, int radix_bits, size_t n,
                                bool is_float, bool allow_skip, unsigned long long* bin_start, SortCtrl* ctrl,
                                cudaStream_t stream) {

@@ -50,6 +50,10 @@ cudaError_t launch_digit_counts(const void* keys, size_t n, int key_bytes, int n
                                 uint32_t shift0, uint32_t shift_step, bool is_float, unsigned long long* out,
                                 cudaStream_t stream);
 
+// Byte counting sort's second step: a[0, n) = each byte value v repeated
+// counts[v] times, in value order (counts: 256 words summing to n).
+cudaError_t launch_counting_fill(uint8_t* a, size_t n, const unsigned long long* counts, cudaStream_t stream);
+
 // Counts of byte `which_byte` of the keys with absolute index in [l, r)
 // (keys points at index l), per work quantum (quantum = index / work_quanta),
 // ADDED into out[quantum][256].

@@ -15,6 +15,7 @@
 #include "HistogramParallel.h"
 #include "RadixSelect.h"
 #include "SumParallel.h"
+#include "CountingSortParallel.h"
 
 static int fail(const char* what) {
   std::printf("FAIL: %s\n", what);
@@ -72,6 +73,16 @@ int main(int argc, char** argv) {
   const unsigned long long sref = std::accumulate(uints.begin(), uints.end(), 0ULL);
   if (ParallelAlgorithms::SumParallelNonRecursive(uints.data(), 0, n) != sref) return fail("SumParallelNonRecursive");
   if ((unsigned long long)ParallelAlgorithms::SumParallel(uints.data(), 0, n) != sref) return fail("SumParallel");
+
+  // counting_sort_parallel vs std::sort of the same bytes
+  {
+    std::vector<unsigned char> bytes(n), want;
+    for (size_t i = 0; i < n; ++i) bytes[i] = (unsigned char)(uints[i] >> 13);
+    want = bytes;
+    std::sort(want.begin(), want.end());
+    ParallelAlgorithms::counting_sort_parallel(bytes.data(), n);
+    if (bytes != want) return fail("counting_sort_parallel");
+  }
 
   std::printf("OK n=%zu\n", n);
   return 0;

@@ -241,3 +241,32 @@ def test_repeated_calls_reuse_workspace(pa, port):
         k = a.copy()
         pa.sort(k)
         np.testing.assert_array_equal(k, want)
+
+
+@pytest.mark.parametrize("n", [0, 1, 15, 16, 17, 4099, 100003, 1 << 20, 10_000_019])
+def test_counting_sort_u8(pa, port, torch_cuda, n):
+    """counting_sort_parallel (CountingSortParallel.h:81) against the oracle:
+    host arrays, uniform / skewed / single-value bytes, and device views that
+    start off a 16-byte boundary (the fill's head and tail bytes)."""
+    rng = np.random.default_rng(4100 + n)
+    cases = {"uniform": rng.integers(0, 256, n, dtype=np.uint8),
+             "skewed": np.minimum(rng.geometric(0.05, n), 255).astype(np.uint8),
+             "single": np.full(n, 77, np.uint8)}
+    for name, a in cases.items():
+        want = port.counting_sort_u8(a)
+        got = a.copy()
+        pa.counting_sort_parallel(got)
+        np.testing.assert_array_equal(got, want, err_msg=name)
+    a = cases["uniform"]
+    if n > 40:
+        l, r = 5, n - 3
+        got = a.copy()
+        pa.counting_sort_parallel_inner(got, l, r)
+        want = a.copy()
+        want[l:r] = port.counting_sort_u8(a[l:r])
+        np.testing.assert_array_equal(got, want)
+        base = torch_cuda.from_numpy(a.copy()).cuda()
+        for off in (1, 7):
+            view = base[off:]
+            pa.counting_sort_parallel(view)
+            np.testing.assert_array_equal(view.cpu().numpy(), port.counting_sort_u8(base.cpu().numpy()[off:]))

@@ -152,3 +152,29 @@ def test_port_select_u64(port):
     s = np.sort(a)
     for k in (0, 17, 5000, 10000):
         assert port.select(a, k) == int(s[k])
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 15, 16, 17, 47, 48, 49, 1000, 4099, 100003])
+def test_counting_sort_and_partition_restatements_match_reference(port, ref, n):
+    """CountingSortParallel.h:29-79 and RadixPartition.h:30-79 restated in C
+    give the compiled reference's result (the partition's exact in-place
+    permutation included)."""
+    rng = np.random.default_rng(4000 + n)
+    b = rng.integers(0, 256, n, dtype=np.uint8)
+    np.testing.assert_array_equal(port.counting_sort_u8(b), np.sort(b))
+    if ref is not None:
+        np.testing.assert_array_equal(ref.counting_sort_u8(b), np.sort(b))
+    u = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    skew = ((rng.integers(0, 4, n, dtype=np.uint64) << 24) | rng.integers(0, 100, n, dtype=np.uint64)).astype(np.uint32)
+    for a in (u, skew):
+        s = np.sort(a)
+        for ks in ([0], [n // 2], [n - 1], sorted({0, n // 3, n // 2, n - 1})):
+            ks = [k for k in ks if 0 <= k < n]
+            if not ks:
+                continue
+            got = port.partition_radix(a, ks)
+            for k in ks:
+                assert got[k] == s[k]
+                assert np.all(got[:k] <= got[k]) and np.all(got[k + 1:] >= got[k])
+            if ref is not None:
+                np.testing.assert_array_equal(got, ref.partition_radix(a, ks))
