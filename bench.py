@@ -619,6 +619,16 @@ def run_extras(pa, lib, _native, workloads, n, stream, peak) -> dict:
                                      "achieved_gbs": 2 * nb / (ms / 1e3) / 1e9,
                                      "frac": 2 * nb / (ms / 1e3) / 1e9 / peak, "sorted": ok}
     del bsrc, bw
+    # PartitionRadix around k = n/2 and n - 21 (RadixPartition.h:152), 100M uniform keys
+    d = dev(workloads.uniform_u32(n))
+    pw = torch.empty_like(d)
+    kk = np.array([n - 21, n // 2], np.uint64)
+    kk.sort()
+    ms = _time_device(lambda: _native.call("pa_partition_radix_u32", P(pw.data_ptr()), n, P(kk.ctypes.data), kk.size,
+                                           o), 5, stream, lambda: pw.copy_(d))
+    out["partition_radix_2k_uniform"] = {"ms": ms, "keys_per_s": n / (ms / 1e3),
+                                         "how": "one GPU sort partitions around every k"}
+    del d, pw
     out["batched_segmented_sort_4096_arrays"] = batched_extra(lib, _native, workloads, stream, peak)
     out["serving_c5"] = serving_extra()
     return out

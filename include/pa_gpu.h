@@ -265,6 +265,16 @@ int pa_server_destroy(pa_server* server);
  * range. */
 int pa_counting_sort_u8(uint8_t* a, size_t n, const pa_opts* opts);
 
+/* Radix partition around the ascending indices k[0, k_len), in place:
+ * replaces PartitionRadix(a, aLength, k[], kLength) (RadixPartition.h:152) and
+ * its single-k and sub-range forms (:92, :124, :165).  Afterwards, for every
+ * k[i], a[k[i]] is the k[i]-th smallest key, no key before it is larger and
+ * no key after it is smaller -- the reference's contract.  The order of the
+ * other keys inside each part differs from the reference's (an artefact of
+ * its serial in-place swap loop): here the whole array comes out sorted, the
+ * GPU's cheapest way to partition around many k at once. */
+int pa_partition_radix_u32(uint32_t* a, size_t n, const size_t* k, size_t k_len, const pa_opts* opts);
+
 /* 256-bin histogram of (key >> shift) & 255 over 64-bit keys (no reference
  * counterpart; the 32-bit form is pa_hist_one_byte_u32). shift < 64. */
 int pa_hist_one_byte_u64(const uint64_t* a, size_t n, unsigned shift, uint64_t* out, const pa_opts* opts);

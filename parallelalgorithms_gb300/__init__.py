@@ -34,7 +34,7 @@ __all__ = [
     "RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase_DeRandomize",
     "HistogramByteComponentsParallel", "HistogramOneByteComponentParallel", "HistogramByteComponentsQCPar",
     "ComputeStartOfBinsPar", "SelectRadix", "SumParallelNonRecursive", "SumParallel",
-    "counting_sort_parallel", "counting_sort_parallel_inner",
+    "counting_sort_parallel", "counting_sort_parallel_inner", "PartitionRadix",
     "sort", "select", "sum_u64", "histogram_digit", "PaError", "lib",
 ]
 
@@ -306,3 +306,46 @@ def counting_sort_parallel(a, a_size: int | None = None) -> None:
     """CountingSortParallel.h:81 counting_sort_parallel(a, a_size): sorts the
     bytes a[0, a_size) in place."""
     counting_sort_parallel_inner(a, 0, _info(a)[1] if a_size is None else a_size)
+
+
+# ---------------------------------------------------------------------------
+# radix partition
+# ---------------------------------------------------------------------------
+def PartitionRadix(a, *args):
+    """RadixPartition.h forms, in place on a uint32 array:
+      PartitionRadix(a, aLength, k) -> a[k]                       (:92)
+      PartitionRadix(a, aStart, aLength, k) -> a[k], k absolute   (:124)
+      PartitionRadix(a, aLength, k_list)                          (:152)
+      PartitionRadix(a, aStart, aLength, k_list, kStart, kLength) (:165)
+    Afterwards every listed a[k] is the k-th smallest of the (sub)range and
+    the range is partitioned around it."""
+    _require_u32(a)
+    if len(args) == 2 and np.ndim(args[1]) == 0:
+        length, k = int(args[0]), int(args[1])
+        _partition(a, 0, length, [k])
+        return int(np.asarray(_fetch(a, k)))
+    if len(args) == 3 and np.ndim(args[2]) == 0:
+        start, length, k = int(args[0]), int(args[1]), int(args[2])
+        _partition(a, start, length, [k])
+        return int(np.asarray(_fetch(a, k)))
+    if len(args) == 2:
+        _partition(a, 0, int(args[0]), list(np.asarray(args[1]).ravel()))
+        return None
+    if len(args) == 5:
+        start, length, ks, kstart, klen = args
+        _partition(a, int(start), int(length), list(np.asarray(ks).ravel()[int(kstart):int(kstart) + int(klen)]))
+        return None
+    raise TypeError("PartitionRadix: unsupported argument list")
+
+
+def _fetch(a, i: int):
+    if _is_torch(a):
+        return int(a[i].item()) & 0xFFFFFFFF
+    return a[i]
+
+
+def _partition(a, start: int, length: int, ks) -> None:
+    """ks: absolute indices inside [start, start + length), ascending."""
+    rel = np.ascontiguousarray([int(k) - start for k in ks], dtype=np.uint64)
+    call("pa_partition_radix_u32", _offset(a, start, 4), length, ctypes.c_void_p(rel.ctypes.data), rel.size,
+         _opts(a))

@@ -738,6 +738,20 @@ int pa_counting_sort_u8(uint8_t* a, size_t n, const pa_opts* opts) {
   return finish(ws, stream, opts && opts->async_device && dev);
 }
 
+int pa_partition_radix_u32(uint32_t* a, size_t n, const size_t* k, size_t k_len, const pa_opts* opts) {
+  if (int rc = check_opts(opts)) return rc;
+  if (k_len == 0 || n == 0) return PA_OK;
+  if (!a || !k) return set_error(PA_ERR_ARG, "NULL buffer");
+  for (size_t i = 0; i < k_len; ++i) {
+    if (k[i] >= n) return set_error(PA_ERR_ARG, "k[%zu] = %zu is not below n = %zu", i, k[i], n);
+    if (i && k[i] < k[i - 1]) return set_error(PA_ERR_ARG, "k[] must be ascending (k[%zu] < k[%zu])", i, i - 1);
+  }
+  // A sorted array is partitioned around every k at once (each a[k[i]] is
+  // the k[i]-th smallest, nothing before it is larger, nothing after it is
+  // smaller), so the whole partition is one GPU sort.
+  return pa_sort_u32(a, nullptr, n, opts);
+}
+
 int pa_hist_quanta_u32(const uint32_t* a, size_t l, size_t r, size_t work_quanta, size_t quanta,
                        unsigned which_byte, uint64_t* out, const pa_opts* opts) {
   if (int rc = check_opts(opts)) return rc;

@@ -16,6 +16,7 @@
 #include "RadixSelect.h"
 #include "SumParallel.h"
 #include "CountingSortParallel.h"
+#include "RadixPartition.h"
 
 static int fail(const char* what) {
   std::printf("FAIL: %s\n", what);
@@ -82,6 +83,21 @@ int main(int argc, char** argv) {
     std::sort(want.begin(), want.end());
     ParallelAlgorithms::counting_sort_parallel(bytes.data(), n);
     if (bytes != want) return fail("counting_sort_parallel");
+  }
+
+  // PartitionRadix around several k: each a[k] is the k-th smallest, parts ordered
+  if (n > 8) {
+    std::vector<unsigned> p(uints), sorted(uints);
+    std::sort(sorted.begin(), sorted.end());
+    size_t ks[3] = {0, n / 3, n - 2};
+    PartitionRadix(p.data(), n, ks, 3);
+    for (size_t k : ks) {
+      if (p[k] != sorted[k]) return fail("PartitionRadix value");
+      for (size_t i = 0; i < k; ++i)
+        if (p[i] > p[k]) return fail("PartitionRadix order");
+    }
+    std::vector<unsigned> q(uints);
+    if (PartitionRadix(q.data(), n, n / 2) != sorted[n / 2]) return fail("PartitionRadix single k");
   }
 
   std::printf("OK n=%zu\n", n);

@@ -270,3 +270,32 @@ def test_counting_sort_u8(pa, port, torch_cuda, n):
             view = base[off:]
             pa.counting_sort_parallel(view)
             np.testing.assert_array_equal(view.cpu().numpy(), port.counting_sort_u8(base.cpu().numpy()[off:]))
+
+
+@pytest.mark.parametrize("n", [1, 2, 48, 100003, 1 << 20])
+def test_partition_radix(pa, port, ref, n):
+    """PartitionRadix (RadixPartition.h:92, :124, :152, :165): every listed
+    a[k] equals the reference's (the k-th smallest), nothing before it is
+    larger and nothing after it is smaller, and the keys are a permutation
+    of the input."""
+    rng = np.random.default_rng(4200 + n)
+    a = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    ks = sorted({0, n // 3, n // 2, n - 1})
+    got = a.copy()
+    pa.PartitionRadix(got, n, np.array(ks, np.uint64))
+    want = port.partition_radix(a, ks)
+    if ref is not None:
+        np.testing.assert_array_equal(want, ref.partition_radix(a, ks))
+    for k in ks:
+        assert got[k] == want[k]
+        assert np.all(got[:k] <= got[k]) and np.all(got[k + 1:] >= got[k])
+    np.testing.assert_array_equal(np.sort(got), np.sort(a))
+    k = n // 2
+    assert pa.PartitionRadix(a.copy(), n, k) == int(np.sort(a)[k])
+    if n > 10:
+        start, length = 3, n - 5
+        c = a.copy()
+        v = pa.PartitionRadix(c, start, length, start + length // 2)
+        assert v == int(np.sort(a[start:start + length])[length // 2])
+        np.testing.assert_array_equal(c[:start], a[:start])
+        np.testing.assert_array_equal(c[start + length:], a[start + length:])
