@@ -265,6 +265,14 @@ int pa_server_destroy(pa_server* server);
  * range. */
 int pa_counting_sort_u8(uint8_t* a, size_t n, const pa_opts* opts);
 
+/* dst = src sorted (stable, ascending); src is clobbered (used as the
+ * scratch).  Replaces the radix-leaf merge sorts that LSD radix sort serves:
+ * parallel_merge_sort_hybrid_radix(src, l, r, dst, srcToDst = true)
+ * (ParallelMergeSort.h:287) and its _single_buffer form (:298); with
+ * srcToDst = false, and parallel_linear_in_place_preventative_adaptive_sort
+ * (:549), they sort in place, which is pa_sort_u32. */
+int pa_sort_copy_u32(uint32_t* src, uint32_t* dst, size_t n, const pa_opts* opts);
+
 /* Radix partition around the ascending indices k[0, k_len), in place:
  * replaces PartitionRadix(a, aLength, k[], kLength) (RadixPartition.h:152) and
  * its single-k and sub-range forms (:92, :124, :165).  Afterwards, for every

@@ -160,6 +160,8 @@ class _Ref:
         h.pa_ref_std_stable_sort_kv_u64.argtypes = [_P, _P, _SZ]
         h.pa_ref_counting_sort_par_u8.argtypes = [_P, _SZ]
         h.pa_ref_partition_radix_u32.argtypes = [_P, _SZ, _P, _SZ]
+        h.pa_ref_merge_sort_hybrid_radix_u32.argtypes = [_P, _SZ, _SZ, _P, ctypes.c_int]
+        h.pa_ref_preventative_adaptive_sort_u32.argtypes = [_P, _SZ]
         self.h = h
 
     def threads(self) -> int:
@@ -238,6 +240,13 @@ class _Ref:
         k = np.ascontiguousarray(ks, dtype=np.uint64)
         self.h.pa_ref_partition_radix_u32(_p(c), c.size, _p(k), k.size)
         return c
+
+    def merge_sort_hybrid_radix(self, src: np.ndarray, l: int, r: int, dst: np.ndarray, src_to_dst: bool) -> None:
+        """In place on src / dst, as the reference (r inclusive)."""
+        self.h.pa_ref_merge_sort_hybrid_radix_u32(_p(src), l, r, _p(dst), int(src_to_dst))
+
+    def preventative_adaptive_sort(self, a: np.ndarray) -> None:
+        self.h.pa_ref_preventative_adaptive_sort_u32(_p(a), a.size)
 
     def std_stable_sort_u64(self, a):
         self.h.pa_ref_std_stable_sort_u64(_p(a), a.size)

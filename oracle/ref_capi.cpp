@@ -141,6 +141,17 @@ void pa_ref_counting_sort_par_u8(unsigned char* a, size_t n) { ParallelAlgorithm
 // radix partition around every k (k ascending).
 void pa_ref_partition_radix_u32(unsigned* a, size_t n, size_t* k, size_t klen) { PartitionRadix(a, n, k, klen); }
 
+// ParallelMergeSort.h:287 parallel_merge_sort_hybrid_radix(src, l, r, dst,
+// srcToDst): merge sort with LSD radix sorted leaves, r inclusive.
+void pa_ref_merge_sort_hybrid_radix_u32(unsigned* src, size_t l, size_t r, unsigned* dst, int src_to_dst) {
+  ParallelAlgorithms::parallel_merge_sort_hybrid_radix(src, l, r, dst, src_to_dst != 0);
+}
+
+// ParallelMergeSort.h:549 parallel_linear_in_place_preventative_adaptive_sort.
+void pa_ref_preventative_adaptive_sort_u32(unsigned* src, size_t n) {
+  ParallelAlgorithms::parallel_linear_in_place_preventative_adaptive_sort(src, n);
+}
+
 // Not in the reference: std::stable_sort baselines for the key types the
 // reference has no radix path for (u64, float32 via its bit pattern, and
 // key + u32 payload pairs).  Float keys are compared by the sign-flipped bit

@@ -35,6 +35,7 @@ __all__ = [
     "HistogramByteComponentsParallel", "HistogramOneByteComponentParallel", "HistogramByteComponentsQCPar",
     "ComputeStartOfBinsPar", "SelectRadix", "SumParallelNonRecursive", "SumParallel",
     "counting_sort_parallel", "counting_sort_parallel_inner", "PartitionRadix",
+    "parallel_merge_sort_hybrid_radix", "parallel_linear_in_place_preventative_adaptive_sort",
     "sort", "select", "sum_u64", "histogram_digit", "PaError", "lib",
 ]
 
@@ -349,3 +350,30 @@ def _partition(a, start: int, length: int, ks) -> None:
     rel = np.ascontiguousarray([int(k) - start for k in ks], dtype=np.uint64)
     call("pa_partition_radix_u32", _offset(a, start, 4), length, ctypes.c_void_p(rel.ctypes.data), rel.size,
          _opts(a))
+
+
+# ---------------------------------------------------------------------------
+# callers that use LSD radix sort as their leaf
+# ---------------------------------------------------------------------------
+def parallel_merge_sort_hybrid_radix(src, l: int, r: int, dst, srcToDst: bool = True,
+                                     parallelThreshold: int = 24 * 1024) -> None:
+    """ParallelMergeSort.h:287: sorts src[l, r] (r INCLUSIVE); the result is
+    in dst[l, r] when srcToDst (src then holds scratch), else in src."""
+    _require_u32(src)
+    n = r - l + 1 if r >= l else 0
+    if n == 0:
+        return
+    if srcToDst:
+        _require_u32(dst)
+        call("pa_sort_copy_u32", _offset(src, l, 4), _offset(dst, l, 4), n, _opts(src, dst))
+    else:
+        call("pa_sort_u32", _offset(src, l, 4), _offset(dst, l, 4) if dst is not None else None, n, _opts(src, dst))
+
+
+def parallel_linear_in_place_preventative_adaptive_sort(src, src_size: int | None = None, stable: bool = True,
+                                                        physical_memory_threshold_post: float = 0.75,
+                                                        parallelThreshold: int = 24 * 1024) -> None:
+    """ParallelMergeSort.h:549: sorts src in place (the GPU's radix sort needs
+    no memory-pressure fallback: device scratch is taken from HBM)."""
+    _require_u32(src)
+    sort(src, n=src_size)

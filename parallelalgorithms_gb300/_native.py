@@ -47,6 +47,7 @@ SIGNATURES: dict[str, list] = {
     "pa_hist_u8": [_P, _SZ, _P, _O],
     "pa_counting_sort_u8": [_P, _SZ, _O],
     "pa_partition_radix_u32": [_P, _SZ, _P, _SZ, _O],
+    "pa_sort_copy_u32": [_P, _P, _SZ, _O],
     "pa_hist_quanta_u32": [_P, _SZ, _SZ, _SZ, _SZ, _U, _P, _O],
     "pa_start_of_bins_u32": [_P, _SZ, _SZ, _SZ, _U, _P, _O],
     "pa_select_u32": [_P, _SZ, _SZ, _P, _O],

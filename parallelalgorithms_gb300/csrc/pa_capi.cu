@@ -738,6 +738,22 @@ int pa_counting_sort_u8(uint8_t* a, size_t n, const pa_opts* opts) {
   return finish(ws, stream, opts && opts->async_device && dev);
 }
 
+int pa_sort_copy_u32(uint32_t* src, uint32_t* dst, size_t n, const pa_opts* opts) {
+  if (int rc = check_opts(opts)) return rc;
+  if (n == 0) return PA_OK;
+  if (!src || !dst) return set_error(PA_ERR_ARG, "NULL buffer");
+  if (src == dst) return pa_sort_u32(dst, nullptr, n, opts);
+  if (int rc = device_ready()) return rc;
+  if (!is_device_ptr(src) && !is_device_ptr(dst)) {
+    std::memcpy(dst, src, n * sizeof(uint32_t));
+  } else {
+    cudaStream_t stream = stream_of(opts);
+    PA_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(uint32_t), cudaMemcpyDefault, stream));
+    if (!is_device_ptr(dst) || !is_device_ptr(src)) PA_CUDA(cudaStreamSynchronize(stream));
+  }
+  return pa_sort_u32(dst, src, n, opts);  // src is the scratch, as in the reference
+}
+
 int pa_partition_radix_u32(uint32_t* a, size_t n, const size_t* k, size_t k_len, const pa_opts* opts) {
   if (int rc = check_opts(opts)) return rc;
   if (k_len == 0 || n == 0) return PA_OK;

@@ -17,6 +17,7 @@
 #include "SumParallel.h"
 #include "CountingSortParallel.h"
 #include "RadixPartition.h"
+#include "ParallelMergeSort.h"
 
 static int fail(const char* what) {
   std::printf("FAIL: %s\n", what);
@@ -98,6 +99,20 @@ int main(int argc, char** argv) {
     }
     std::vector<unsigned> q(uints);
     if (PartitionRadix(q.data(), n, n / 2) != sorted[n / 2]) return fail("PartitionRadix single k");
+  }
+
+  // the radix-leaf merge sorts: result in dst (srcToDst) or in src
+  if (n > 2) {
+    std::vector<unsigned> sorted(uints), src(uints), dst(n, 0u);
+    std::sort(sorted.begin(), sorted.end());
+    ParallelAlgorithms::parallel_merge_sort_hybrid_radix(src.data(), 0, n - 1, dst.data(), true);
+    if (dst != sorted) return fail("parallel_merge_sort_hybrid_radix(srcToDst)");
+    std::vector<unsigned> src2(uints), work(n);
+    ParallelAlgorithms::parallel_merge_sort_hybrid_radix(src2.data(), 0, n - 1, work.data(), false);
+    if (src2 != sorted) return fail("parallel_merge_sort_hybrid_radix(in src)");
+    std::vector<unsigned> src3(uints);
+    ParallelAlgorithms::parallel_linear_in_place_preventative_adaptive_sort(src3.data(), n);
+    if (src3 != sorted) return fail("parallel_linear_in_place_preventative_adaptive_sort");
   }
 
   std::printf("OK n=%zu\n", n);

@@ -299,3 +299,35 @@ def test_partition_radix(pa, port, ref, n):
         assert v == int(np.sort(a[start:start + length])[length // 2])
         np.testing.assert_array_equal(c[:start], a[:start])
         np.testing.assert_array_equal(c[start + length:], a[start + length:])
+
+
+@pytest.mark.parametrize("n", [1, 2, 100003, 1 << 20])
+def test_radix_leaf_merge_sorts(pa, ref, torch_cuda, n):
+    """parallel_merge_sort_hybrid_radix (ParallelMergeSort.h:287) with the
+    result in dst or in src, on a sub-range, and
+    parallel_linear_in_place_preventative_adaptive_sort (:549): the same
+    sorted keys as the compiled reference."""
+    rng = np.random.default_rng(4400 + n)
+    a = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    want = np.sort(a)
+    if ref is not None:
+        s_ref, d_ref = a.copy(), np.zeros_like(a)
+        ref.merge_sort_hybrid_radix(s_ref, 0, n - 1, d_ref, True)
+        np.testing.assert_array_equal(d_ref, want)
+    src, dst = a.copy(), np.zeros_like(a)
+    pa.parallel_merge_sort_hybrid_radix(src, 0, n - 1, dst, True)
+    np.testing.assert_array_equal(dst, want)
+    src, work = a.copy(), np.zeros_like(a)
+    pa.parallel_merge_sort_hybrid_radix(src, 0, n - 1, work, False)
+    np.testing.assert_array_equal(src, want)
+    c = a.copy()
+    pa.parallel_linear_in_place_preventative_adaptive_sort(c)
+    np.testing.assert_array_equal(c, want)
+    if n > 10:  # sub-range [l, r] inclusive, device buffers
+        l, r = 3, n - 4
+        ds = torch_cuda.from_numpy(a.view(np.int32).copy()).cuda()
+        dd = torch_cuda.zeros_like(ds)
+        pa.parallel_merge_sort_hybrid_radix(ds, l, r, dd, True)
+        got = dd.cpu().numpy().view(np.uint32)
+        np.testing.assert_array_equal(got[l:r + 1], np.sort(a[l:r + 1]))
+        assert not got[:l].any() and not got[r + 1:].any()

@@ -178,3 +178,22 @@ def test_counting_sort_and_partition_restatements_match_reference(port, ref, n):
                 assert np.all(got[:k] <= got[k]) and np.all(got[k + 1:] >= got[k])
             if ref is not None:
                 np.testing.assert_array_equal(got, ref.partition_radix(a, ks))
+
+
+@pytest.mark.parametrize("n", [1, 2, 100, 100003])
+def test_reference_merge_sorts_sort(ref, n):
+    """The reference's radix-leaf merge sorts, compiled unchanged, sort (the
+    GPU drop-ins are checked against the same sorted result)."""
+    if ref is None:
+        pytest.skip("reference not built")
+    rng = np.random.default_rng(4300 + n)
+    a = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    src, dst = a.copy(), np.zeros_like(a)
+    ref.merge_sort_hybrid_radix(src, 0, n - 1, dst, True)
+    np.testing.assert_array_equal(dst, np.sort(a))
+    src, work = a.copy(), np.zeros_like(a)
+    ref.merge_sort_hybrid_radix(src, 0, n - 1, work, False)
+    np.testing.assert_array_equal(src, np.sort(a))
+    c = a.copy()
+    ref.preventative_adaptive_sort(c)
+    np.testing.assert_array_equal(c, np.sort(a))
