@@ -1,0 +1,22 @@
+// Drop-in replacement for the reference's RadixSortMsdParallel.h entry point:
+// in-place sort of unsigned keys.  The reference's MSD sort is unstable; for
+// keys alone any sort gives the same array, here the GPU LSD radix sort.
+#ifndef PA_DROPIN_RADIXSORTMSDPARALLEL_H
+#define PA_DROPIN_RADIXSORTMSDPARALLEL_H
+
+#include <cstddef>
+#include <cstdint>
+
+#include "pa_dropin_common.h"
+
+namespace ParallelAlgorithms {
+
+// RadixSortMsdParallel.h:291
+inline void parallel_hybrid_inplace_msd_radix_sort(unsigned* a, size_t a_size) {
+  if (a_size < 2) return;
+  pa_detail::check(pa_sort_u32(a, nullptr, a_size, nullptr), "parallel_hybrid_inplace_msd_radix_sort");
+}
+
+}  // namespace ParallelAlgorithms
+
+#endif

@@ -162,6 +162,7 @@ class _Ref:
         h.pa_ref_partition_radix_u32.argtypes = [_P, _SZ, _P, _SZ]
         h.pa_ref_merge_sort_hybrid_radix_u32.argtypes = [_P, _SZ, _SZ, _P, ctypes.c_int]
         h.pa_ref_preventative_adaptive_sort_u32.argtypes = [_P, _SZ]
+        h.pa_ref_msd_radix_sort_u32.argtypes = [_P, _SZ]
         self.h = h
 
     def threads(self) -> int:
@@ -244,6 +245,9 @@ class _Ref:
     def merge_sort_hybrid_radix(self, src: np.ndarray, l: int, r: int, dst: np.ndarray, src_to_dst: bool) -> None:
         """In place on src / dst, as the reference (r inclusive)."""
         self.h.pa_ref_merge_sort_hybrid_radix_u32(_p(src), l, r, _p(dst), int(src_to_dst))
+
+    def msd_radix_sort(self, a: np.ndarray) -> None:
+        self.h.pa_ref_msd_radix_sort_u32(_p(a), a.size)
 
     def preventative_adaptive_sort(self, a: np.ndarray) -> None:
         self.h.pa_ref_preventative_adaptive_sort_u32(_p(a), a.size)

@@ -152,6 +152,9 @@ void pa_ref_preventative_adaptive_sort_u32(unsigned* src, size_t n) {
   ParallelAlgorithms::parallel_linear_in_place_preventative_adaptive_sort(src, n);
 }
 
+// RadixSortMsdParallel.h:291 parallel_hybrid_inplace_msd_radix_sort(a, n).
+void pa_ref_msd_radix_sort_u32(unsigned* a, size_t n) { ParallelAlgorithms::parallel_hybrid_inplace_msd_radix_sort(a, n); }
+
 // Not in the reference: std::stable_sort baselines for the key types the
 // reference has no radix path for (u64, float32 via its bit pattern, and
 // key + u32 payload pairs).  Float keys are compared by the sign-flipped bit

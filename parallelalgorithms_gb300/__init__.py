@@ -36,6 +36,7 @@ __all__ = [
     "ComputeStartOfBinsPar", "SelectRadix", "SumParallelNonRecursive", "SumParallel",
     "counting_sort_parallel", "counting_sort_parallel_inner", "PartitionRadix",
     "parallel_merge_sort_hybrid_radix", "parallel_linear_in_place_preventative_adaptive_sort",
+    "parallel_hybrid_inplace_msd_radix_sort",
     "sort", "select", "sum_u64", "histogram_digit", "PaError", "lib",
 ]
 
@@ -377,3 +378,12 @@ def parallel_linear_in_place_preventative_adaptive_sort(src, src_size: int | Non
     no memory-pressure fallback: device scratch is taken from HBM)."""
     _require_u32(src)
     sort(src, n=src_size)
+
+
+def parallel_hybrid_inplace_msd_radix_sort(a, a_size: int | None = None) -> None:
+    """RadixSortMsdParallel.h:291: sorts a[0, a_size) in place (for keys
+    alone the unstable MSD sort and this LSD sort give the same array)."""
+    _require_u32(a)
+    n = _info(a)[1] if a_size is None else a_size
+    if n >= 2:
+        sort(a, n=n)

@@ -18,6 +18,7 @@
 #include "CountingSortParallel.h"
 #include "RadixPartition.h"
 #include "ParallelMergeSort.h"
+#include "RadixSortMsdParallel.h"
 
 static int fail(const char* what) {
   std::printf("FAIL: %s\n", what);
@@ -113,6 +114,9 @@ int main(int argc, char** argv) {
     std::vector<unsigned> src3(uints);
     ParallelAlgorithms::parallel_linear_in_place_preventative_adaptive_sort(src3.data(), n);
     if (src3 != sorted) return fail("parallel_linear_in_place_preventative_adaptive_sort");
+    std::vector<unsigned> src4(uints);
+    ParallelAlgorithms::parallel_hybrid_inplace_msd_radix_sort(src4.data(), n);
+    if (src4 != sorted) return fail("parallel_hybrid_inplace_msd_radix_sort");
   }
 
   std::printf("OK n=%zu\n", n);

@@ -323,6 +323,13 @@ def test_radix_leaf_merge_sorts(pa, ref, torch_cuda, n):
     c = a.copy()
     pa.parallel_linear_in_place_preventative_adaptive_sort(c)
     np.testing.assert_array_equal(c, want)
+    c = a.copy()
+    pa.parallel_hybrid_inplace_msd_radix_sort(c)
+    np.testing.assert_array_equal(c, want)
+    if ref is not None:
+        m = a.copy()
+        ref.msd_radix_sort(m)
+        np.testing.assert_array_equal(m, want)
     if n > 10:  # sub-range [l, r] inclusive, device buffers
         l, r = 3, n - 4
         ds = torch_cuda.from_numpy(a.view(np.int32).copy()).cuda()

@@ -197,3 +197,6 @@ def test_reference_merge_sorts_sort(ref, n):
     c = a.copy()
     ref.preventative_adaptive_sort(c)
     np.testing.assert_array_equal(c, np.sort(a))
+    c = a.copy()
+    ref.msd_radix_sort(c)
+    np.testing.assert_array_equal(c, np.sort(a))
