@@ -186,7 +186,8 @@ bool use_multisplit() {
 template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S>
 cudaError_t launch_g(const OnesweepArgs& a, cudaStream_t stream) {
   if (use_multisplit()) return launch_g2<K, HAS_VALS, BLOCK, ITEMS, MINB, S, true>(a, stream);
-  return launch_g2<K, HAS_VALS, BLOCK, ITEMS, MINB, S, false>(a, stream);
+  if constexpr (ITEMS <= 16) return launch_g2<K, HAS_VALS, BLOCK, ITEMS, MINB, S, false>(a, stream);
+  return cudaErrorInvalidConfiguration;  // the counting ranking packs ranks in 4 bits (at most 16 items)
 }
 
 template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB>

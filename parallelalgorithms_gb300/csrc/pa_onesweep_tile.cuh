@@ -55,7 +55,6 @@ struct Geometry {
   static_assert(kTile % 4 == 0, "tile starts must stay 16-byte aligned");
   static_assert((ITEMS * sizeof(K)) % 16 == 0, "a thread's run of keys is read as 16-byte vectors");
   static_assert(BLOCK >= kRadix, "one thread per bin in the look-back");
-  static_assert(ITEMS <= 16, "per-thread ranks are packed in 4 bits");
 };
 
 // Block-wide exclusive scan of one value per thread.  Contains one
@@ -216,6 +215,7 @@ template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, typename S>
 __device__ __forceinline__ void onesweep_tile(const TileJob<K, S>& job, unsigned char* smem, uint64_t* s_bar,
                                               uint32_t& parity) {
   using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
+  static_assert(ITEMS <= 16, "per-thread ranks are packed in 4 bits");
   using SW = StatusWord<S>;
   constexpr int TILE = G::kTile;
   K* s_keys = reinterpret_cast<K*>(smem + G::kKeysOff);
