@@ -1,7 +1,7 @@
 """CPU checkers for the GB300 radix hot path -- TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
-arm may import this package, and only as the checker or the timed CPU
+arm may import this package, and only to check results or as the timed CPU
 baseline.  The product path (parallelalgorithms_gb300) never imports it.
 
 Two checkers:

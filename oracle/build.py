@@ -9,8 +9,8 @@
 The reference headers are read from /root/reference when it exists; the
 include closure of ref_capi.cpp is also staged (unmodified, never committed:
 oracle/_ref/ is git-ignored) in oracle/_ref/src/, so that a machine without
-/root/reference (the GPU host, an aarch64 machine on which x86 objects cannot
-run) rebuilds the same reference code from there.  Nothing here is run by
+/root/reference (such as an aarch64 host, on which x86 objects cannot run)
+rebuilds the same reference code from there.  Nothing here is run by
 the product path.
 """
 from __future__ import annotations

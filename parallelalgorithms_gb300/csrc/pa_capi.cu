@@ -15,7 +15,9 @@
 #include <functional>
 #include <map>
 #include <mutex>
+#include <set>
 #include <string>
+#include <tuple>
 #include <utility>
 
 #include "pa_gpu.h"
@@ -189,22 +191,20 @@ constexpr size_t kPipeMinKeys = (size_t)1 << 24;
 // Groups per pipelined sort (at most kPipeGroups; PA_HOST_PIPELINE_GROUPS
 // overrides the default for tuning).
 int pipe_groups() {
-  static int v = -1;
-  if (v < 0) {
+  static const int v = [] {  // read once (thread-safe initialisation)
     const char* e = std::getenv("PA_HOST_PIPELINE_GROUPS");
-    v = e ? std::atoi(e) : kPipeGroups;
-    if (v < 1 || v > kPipeGroups) v = kPipeGroups;
-  }
+    const int g = e ? std::atoi(e) : kPipeGroups;
+    return (g < 1 || g > kPipeGroups) ? kPipeGroups : g;
+  }();
   return v;
 }
 
 bool pipeline_enabled() {
-  static int v = -1;
-  if (v < 0) {
+  static const bool v = [] {
     const char* e = std::getenv("PA_HOST_PIPELINE");
-    v = (e && std::strcmp(e, "0") == 0) ? 0 : 1;
-  }
-  return v == 1;
+    return !(e && std::strcmp(e, "0") == 0);
+  }();
+  return v;
 }
 
 int pipelined_host_sort(Workspace* ws, cudaStream_t stream, void* keys, size_t n, int kb) {
@@ -576,9 +576,11 @@ int record_error(int status, const char* message) { return set_error(status, "%s
 
 const DeviceInfo& device_info() {
   static DeviceInfo infos[64];
+  static std::mutex mu;
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
+  std::lock_guard<std::mutex> lk(mu);  // launches come from callers' threads and the server's thread
   DeviceInfo& d = infos[dev];
   if (d.device != dev) {
     int sms = 0, smem = 0;
@@ -589,6 +591,20 @@ const DeviceInfo& device_info() {
     d.device = dev;
   }
   return d;
+}
+
+cudaError_t ensure_dynamic_smem(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::set<std::tuple<int, const void*, size_t>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_tuple(dev, func, bytes);
+  if (done.count(key)) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) done.insert(key);
+  return e;
 }
 
 }  // namespace pa

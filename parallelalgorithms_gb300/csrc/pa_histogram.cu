@@ -105,12 +105,8 @@ cudaError_t launch_counts_t(const void* keys, size_t n, uint32_t shift0, uint32_
   constexpr int V = kVec<K>;
   auto kern = digit_counts_kernel<K, ND, RB>;
   constexpr size_t smem = hist_smem_bytes<ND, RB>();
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  cudaError_t e = ensure_dynamic_smem(kern, smem);
+  if (e != cudaSuccess) return e;
   const size_t work = ceil_div(ceil_div(n, (size_t)V), (size_t)kHistBlock * 4);
   size_t blocks = work < (size_t)device_info().sm_count ? work : (size_t)device_info().sm_count;
   if (blocks < 1) blocks = 1;

@@ -42,6 +42,14 @@ struct DeviceInfo {
 };
 const DeviceInfo& device_info();
 
+// Lets `func` use `bytes` of dynamic shared memory on the current device:
+// cudaFuncSetAttribute once per (device, function), thread-safe.
+cudaError_t ensure_dynamic_smem(const void* func, size_t bytes);
+template <typename F>
+cudaError_t ensure_dynamic_smem(F* func, size_t bytes) {
+  return ensure_dynamic_smem(reinterpret_cast<const void*>(func), bytes);
+}
+
 // ---- histograms (pa_histogram.cu) -----------------------------------------
 // Counts of `num_digits` digits of width `radix_bits` (digit d taken at bit
 // shift0 + d * shift_step of the ordered key) over keys[0, n), ADDED into

@@ -138,11 +138,10 @@ constexpr GeomChoice kGeomU64[] = {{512, 12, 2}, {256, 12, 4}, {512, 8, 3}};
 constexpr GeomChoice kGeomU64Kv[] = {{256, 12, 3}, {256, 8, 4}, {512, 8, 2}};
 
 int geometry_index(int count) {
-  static int idx = -2;
-  if (idx == -2) {
+  static const int idx = [] {  // read once (thread-safe initialisation)
     const char* e = std::getenv("PA_ONESWEEP_GEOMETRY");
-    idx = e ? std::atoi(e) : 0;
-  }
+    return e ? std::atoi(e) : 0;
+  }();
   return (idx >= 0 && idx < count) ? idx : 0;
 }
 
@@ -158,12 +157,8 @@ template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S,
 cudaError_t launch_g2(const OnesweepArgs& a, cudaStream_t stream) {
   using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
   auto kern = onesweep_kernel<K, HAS_VALS, BLOCK, ITEMS, MINB, S, MS>;
-  static bool configured = false;  // one attribute call per instantiation
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kBytes);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  cudaError_t e = ensure_dynamic_smem(kern, G::kBytes);
+  if (e != cudaSuccess) return e;
   const size_t tiles = ceil_div(a.n, (size_t)G::kTile);
   kern<<<(unsigned)tiles, BLOCK, G::kBytes, stream>>>(a);
   return cudaGetLastError();
@@ -175,12 +170,11 @@ cudaError_t launch_g2(const OnesweepArgs& a, cudaStream_t stream) {
 // current one was measured slower on GB300 (tickets taken early make
 // successors wait in the look-back) and is not built.
 bool use_multisplit() {
-  static int v = -1;
-  if (v < 0) {
+  static const bool v = [] {
     const char* e = std::getenv("PA_ONESWEEP_RANK");
-    v = (e && std::strcmp(e, "counting") == 0) ? 0 : 1;
-  }
-  return v == 1;
+    return !(e && std::strcmp(e, "counting") == 0);
+  }();
+  return v;
 }
 
 template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S>

@@ -349,13 +349,7 @@ cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s, void* pin
 }
 
 unsigned plan_grid(const HostPlan& hp) {
-  static bool configured[2][3] = {};
-  const int pi = hp.kc.pass_tile == 4096 ? 0 : 1;
-  const int si = hp.kc.small_tile == 2048 ? 0 : hp.kc.small_tile == 4096 ? 1 : 2;
-  if (!configured[pi][si]) {
-    cudaFuncSetAttribute(hp.kc.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hp.kc.smem);
-    configured[pi][si] = true;
-  }
+  if (ensure_dynamic_smem(hp.kc.fn, hp.kc.smem) != cudaSuccess) cudaGetLastError();  // the launch reports it
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hp.kc.fn, kBlock, hp.kc.smem) != cudaSuccess) {
     cudaGetLastError();

@@ -262,12 +262,8 @@ cudaError_t launch_select_t(const K* keys, size_t n, K* cand, size_t cand_cap, S
   select_pick_kernel<K><<<1, 256, 0, stream>>>(st, out);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  static bool configured = false;
-  if (!configured) {
-    e = cudaFuncSetAttribute(select_step_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Ring::kBytes);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  e = ensure_dynamic_smem(select_step_kernel<K>, Ring::kBytes);
+  if (e != cudaSuccess) return e;
   const unsigned grid = (unsigned)max(1, device_info().sm_count * 2);  // two CTAs per SM
   for (uint32_t s = 1; s < W / 8; ++s) {
     const uint32_t shift = W - 8u * (s + 1);

@@ -79,12 +79,8 @@ __global__ void __launch_bounds__(Ring::kThreads, 1) sum_kernel(const K* __restr
 template <typename K>
 cudaError_t launch_sum_t(const K* keys, size_t n, unsigned long long* partials, uint32_t* ticket,
                          unsigned long long* out, uint32_t* err, cudaStream_t stream) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(sum_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Ring::kBytes);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  cudaError_t e = ensure_dynamic_smem(sum_kernel<K>, Ring::kBytes);
+  if (e != cudaSuccess) return e;
   const size_t chunks = ceil_div(n * sizeof(K), (size_t)kChunk);
   size_t blocks = min((size_t)device_info().sm_count, (size_t)kMaxSumBlocks);
   if (blocks > chunks) blocks = chunks;
