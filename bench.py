@@ -46,6 +46,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "uint32 keys/s sorted at 100M vs HBM roofline; batched/served keys/s + p99 latency"
 UNIT = "keys/s"
+# The reference's published figure for this metric: parallel LSD radix sort of
+# 100,000,000 random uint32 keys, 2865 M keys/s on a 48-core AWS c7a.24xlarge
+# (the reference README's table, its fastest published machine).
+PUBLISHED_KEYS_PER_S = 2.865e9
+PUBLISHED_SOURCE = "reference README: parallel LSD radix sort, 100M random uint32, 48-core AWS c7a.24xlarge"
 PROFILE_TRAFFIC = ROOT / "profiles" / "onesweep_pass_u32_100m_traffic.txt"
 
 
@@ -228,7 +233,8 @@ def reference_arm(args) -> None:
     med_s = args.n / cb["value"]
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": med_s * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": cb["value"] / PUBLISHED_KEYS_PER_S, "vs_baseline_source": PUBLISHED_SOURCE,
+            "dtype": "u32", "data": "synthetic",
             "config": {"workload": f"LSD radix sort of {args.n} uniform uint32 keys, 8-bit digits",
                        "keys": args.n, "key_type": "uint32", "distribution": "uniform mt19937_64(1234)",
                        "l2": "inputs (400 MB) larger than L2"},
@@ -362,7 +368,8 @@ def gb300_arm(args) -> None:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "vs_baseline": value / PUBLISHED_KEYS_PER_S, "vs_baseline_source": PUBLISHED_SOURCE,
+            "dtype": "u32", "data": "synthetic",
             "config": {"workload": f"LSD radix sort of {n} uniform uint32 keys (mt19937_64 seed 1234), "
                                    "8-bit digits, 4 passes, device-resident",
                        "keys_per_gpu": n, "key_type": "uint32", "digit_bits": 8,
