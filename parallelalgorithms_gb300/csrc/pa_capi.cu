@@ -207,8 +207,19 @@ bool pipeline_enabled() {
   return v;
 }
 
+// Host-side fault injection for tests: PA_FAULT_PIPELINE_OOM=1 makes the
+// pipelined sort report a device allocation failure before it allocates.
+bool fault_pipeline_oom() {
+  static const bool v = [] {
+    const char* e = std::getenv("PA_FAULT_PIPELINE_OOM");
+    return e && std::strcmp(e, "1") == 0;
+  }();
+  return v;
+}
+
 int pipelined_host_sort(Workspace* ws, cudaStream_t stream, void* keys, size_t n, int kb) {
   static_assert(kPipeChunks <= 16, "a group gathers at most 16 pieces");
+  if (fault_pipeline_oom()) return set_error(PA_ERR_OOM, "injected allocation failure (PA_FAULT_PIPELINE_OOM)");
   constexpr size_t kHostWords = (size_t)kPipeChunks * 256 + (size_t)kPipeGroups * kPipeChunks * 2;
   if (!ws->copy_stream) PA_CUDA(cudaStreamCreateWithFlags(&ws->copy_stream, cudaStreamNonBlocking));
   for (auto& e : ws->pipe_ev)
@@ -344,14 +355,15 @@ int sort_impl(void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t 
   const bool tmp_dev = is_device_ptr(tmp);
   if (!keys_dev && !has_vals && !is_float && !(phase_ms && phase_cap > 0) && n >= kPipeMinKeys &&
       pipeline_enabled()) {
-    if (int rc = pipelined_host_sort(ws, stream, keys, n, kb)) {
-      // nothing may still copy into the caller's buffer after the call returns
-      if (ws->copy_stream) cudaStreamSynchronize(ws->copy_stream);
-      cudaStreamSynchronize(stream);
-      cudaGetLastError();
-      return rc;
-    }
-    return finish(ws, stream, false);
+    const int rc = pipelined_host_sort(ws, stream, keys, n, kb);
+    if (rc == PA_OK) return finish(ws, stream, false);
+    // nothing may still copy into the caller's buffer after the call returns
+    if (ws->copy_stream) cudaStreamSynchronize(ws->copy_stream);
+    cudaStreamSynchronize(stream);
+    cudaGetLastError();
+    // the pipeline needs a third key-sized device buffer; without the memory
+    // for it, the plain host path below (two buffers) still sorts
+    if (rc != PA_ERR_OOM) return rc;
   }
   const bool vals_dev = has_vals && is_device_ptr(vals);
   const bool tvals_dev = has_vals && is_device_ptr(tmp_vals);

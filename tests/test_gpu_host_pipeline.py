@@ -52,3 +52,29 @@ def test_pipelined_equals_device_sort_100m(pa, torch_cuda):
     host = a.copy()
     pa.sort(host)
     np.testing.assert_array_equal(host, d.cpu().numpy().view(np.uint32))
+
+
+def test_pipeline_out_of_memory_falls_back_to_the_plain_host_sort(tmp_path):
+    """With the pipeline's allocation failing (host-side fault injection),
+    the same call still sorts through the two-buffer host path."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    script = tmp_path / "oom_fallback.py"
+    script.write_text(
+        "import sys\n"
+        f"sys.path.insert(0, {str(root)!r})\n"
+        "import numpy as np\n"
+        "import parallelalgorithms_gb300 as pa\n"
+        "from parallelalgorithms_gb300 import workloads\n"
+        f"a = workloads.uniform_u32({N})\n"
+        "got = a.copy()\n"
+        "pa.sort(got)\n"
+        "assert np.array_equal(got, np.sort(a))\n"
+        "print('fallback ok')\n")
+    env = dict(os.environ, PA_FAULT_PIPELINE_OOM="1")
+    r = subprocess.run([sys.executable, str(script)], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "fallback ok" in r.stdout
