@@ -555,6 +555,15 @@ cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32
   const int passes = kb;
   const bool has_vals = d_vals != nullptr;
   auto m = [&]() { return mark ? mark() : cudaSuccess; };
+  if (n <= small_sort_max_keys(kb, has_vals)) {  // one CTA, one launch
+    (void)d_tmp;
+    (void)d_tvals;
+    (void)err;
+    cudaError_t e = m();
+    if (e == cudaSuccess) e = launch_small_sort(d_keys, d_vals, n, kb, is_float, stream);
+    if (e == cudaSuccess) e = m();
+    return e;
+  }
   cudaError_t e = cudaMemsetAsync(s.zero_begin, 0, s.zero_bytes, stream);
   if (e == cudaSuccess) e = m();
   if (e == cudaSuccess) e = launch_digit_counts(d_keys, n, kb, passes, 8, 0, 8, is_float, s.counts, stream);

@@ -104,6 +104,11 @@ size_t onesweep_tile_keys(int key_bytes, bool has_vals);
 size_t onesweep_status_bytes(size_t n);
 cudaError_t launch_onesweep_pass(const OnesweepArgs& a, int key_bytes, bool has_vals, cudaStream_t stream);
 
+// Whole sort of n <= small_sort_max_keys(key_bytes, has_vals) keys (and
+// payloads) by one CTA in shared memory, in place.
+size_t small_sort_max_keys(int key_bytes, bool has_vals);
+cudaError_t launch_small_sort(void* keys, uint32_t* vals, size_t n, int key_bytes, bool is_float, cudaStream_t stream);
+
 // dst[0, total) = the concatenation of `npieces` runs of src, piece i being
 // src[pieces[2i], pieces[2i] + pieces[2i + 1]) (element offsets and counts;
 // npieces <= 16).  key_bytes 4 or 8.

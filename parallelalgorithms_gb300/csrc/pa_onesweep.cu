@@ -83,6 +83,52 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
     onesweep_tile<K, HAS_VALS, BLOCK, ITEMS, S>(job, smem, s_bar, parity);
 }
 
+// A whole sort of at most BLOCK * ITEMS keys by one CTA, in shared memory:
+// the keys (and payloads) are read once, sorted by stable 4-bit counting
+// passes over every nibble (each thread owns ITEMS consecutive keys, so
+// (thread, item) order is input order), and written once.  One launch
+// instead of the histogram / scan / digit-pass chain, for small inputs
+// whose cost is launch latency.  Padding keys (all ones) sort after every
+// real key.
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK, 1) small_sort_kernel(K* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                             uint32_t n, int is_float) {
+  using G = Geometry<K, HAS_VALS, BLOCK, ITEMS>;
+  constexpr int TILE = G::kTile;
+  extern __shared__ __align__(128) unsigned char smem[];
+  K* s_keys = reinterpret_cast<K*>(smem + G::kKeysOff);
+  uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + G::kValsOff);
+  uint32_t* s_cnt = reinterpret_cast<uint32_t*>(smem + G::kCntOff);
+  uint32_t* s_warp = reinterpret_cast<uint32_t*>(smem + G::kWarpTotOff);
+  const bool flt = is_float != 0;
+  for (uint32_t i = threadIdx.x; i < (uint32_t)TILE; i += BLOCK) {
+    s_keys[i] = i < n ? to_ordered(keys[i], flt) : ~(K)0;
+    if (HAS_VALS) s_vals[i] = i < n ? vals[i] : 0u;
+  }
+  __syncthreads();
+  K k[ITEMS];
+  uint32_t v[HAS_VALS ? ITEMS : 1];
+  for (uint32_t sh = 0; sh < 8u * (uint32_t)sizeof(K); sh += 4) {
+    load_run<K, HAS_VALS, ITEMS>(k, v, s_keys, s_vals);
+    nibble_pass<K, HAS_VALS, BLOCK, ITEMS>(k, v, sh, s_keys, s_vals, s_cnt, s_warp);  // ends with a barrier
+  }
+  for (uint32_t i = threadIdx.x; i < n; i += BLOCK) {
+    keys[i] = from_ordered(s_keys[i], flt);
+    if (HAS_VALS) vals[i] = s_vals[i];
+  }
+}
+
+template <typename K, bool HAS_VALS, int ITEMS>
+cudaError_t launch_small_t(void* keys, uint32_t* vals, size_t n, bool is_float, cudaStream_t stream) {
+  constexpr int kSmallBlock = 512;
+  using G = Geometry<K, HAS_VALS, kSmallBlock, ITEMS>;
+  auto kern = small_sort_kernel<K, HAS_VALS, kSmallBlock, ITEMS>;
+  cudaError_t e = ensure_dynamic_smem(kern, G::kBytes);
+  if (e != cudaSuccess) return e;
+  kern<<<1, kSmallBlock, G::kBytes, stream>>>(static_cast<K*>(keys), vals, (uint32_t)n, is_float ? 1 : 0);
+  return cudaGetLastError();
+}
+
 template <typename K>
 __global__ void final_copy_kernel(K* keys_a, const K* keys_b, uint32_t* vals_a, const uint32_t* vals_b, size_t n,
                                   const SortCtrl* ctrl) {
@@ -235,6 +281,23 @@ cudaError_t launch_onesweep_pass(const OnesweepArgs& a, int key_bytes, bool has_
   if (a.n == 0) return cudaSuccess;
   if (key_bytes == 4) return has_vals ? launch_kv<uint32_t, true>(a, stream) : launch_kv<uint32_t, false>(a, stream);
   return has_vals ? launch_kv<unsigned long long, true>(a, stream) : launch_kv<unsigned long long, false>(a, stream);
+}
+
+size_t small_sort_max_keys(int key_bytes, bool has_vals) {
+  (void)has_vals;
+  return key_bytes == 4 ? 512 * 16 : 512 * 8;
+}
+
+cudaError_t launch_small_sort(void* keys, uint32_t* vals, size_t n, int key_bytes, bool is_float, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  if (n > small_sort_max_keys(key_bytes, vals != nullptr)) return cudaErrorInvalidValue;
+  if (key_bytes == 4)
+    return vals ? launch_small_t<uint32_t, true, 16>(keys, vals, n, is_float, stream)
+                : launch_small_t<uint32_t, false, 16>(keys, vals, n, is_float, stream);
+  if (key_bytes == 8)
+    return vals ? launch_small_t<unsigned long long, true, 8>(keys, vals, n, false, stream)
+                : launch_small_t<unsigned long long, false, 8>(keys, vals, n, false, stream);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_gather_pieces(const void* src, void* dst, const unsigned long long* pieces, int npieces,

@@ -54,7 +54,7 @@ def test_sort_u32_host_and_device_match_oracle(pa, port, torch_cuda, n):
         np.testing.assert_array_equal(from_dev(d, np.uint32), want, err_msg=f"device {name} n={n}")
 
 
-@pytest.mark.parametrize("n", [1, 100, 4097, 6144, 6145, 65537, 1 << 20])
+@pytest.mark.parametrize("n", [1, 100, 4097, 6144, 6145, 8192, 8193, 65537, 1 << 20])
 def test_sort_kv_u32_stable(pa, port, n):
     for name, a in u32_inputs(n).items():
         vals = np.arange(n, dtype=np.uint32)
@@ -65,7 +65,7 @@ def test_sort_kv_u32_stable(pa, port, n):
         np.testing.assert_array_equal(v, wv, err_msg=name)
 
 
-@pytest.mark.parametrize("n", [1, 99, 4096, 6143, 6144, 6145, 100003, 1 << 20])
+@pytest.mark.parametrize("n", [1, 99, 4096, 4097, 6143, 6144, 6145, 100003, 1 << 20])
 def test_sort_u64_and_kv_u64(pa, port, n):
     from parallelalgorithms_gb300 import workloads
     rng = np.random.default_rng(7 + n)
@@ -89,7 +89,7 @@ def test_sort_u64_and_kv_u64(pa, port, n):
         np.testing.assert_array_equal(v, wv, err_msg=name)
 
 
-@pytest.mark.parametrize("n", [1, 2, 100, 8193, 100003, 1 << 20])
+@pytest.mark.parametrize("n", [1, 2, 100, 8192, 8193, 100003, 1 << 20])
 def test_sort_f32_total_order_and_payload(pa, port, torch_cuda, n):
     from parallelalgorithms_gb300 import workloads
     a = workloads.normal_specials_f32(n)
