@@ -13,6 +13,9 @@
 // in distinct banks whatever the key distribution (constant input included).
 // A CTA streams a grid-strided share of the keys with 16-byte loads, then
 // folds the lane copies and adds its counts into the 64-bit global result.
+//
+// Also here: the per-quantum counts and start of bins (ComputeStartOfBinsPar),
+// the scan + pass control of the sort, and the byte counting sort's fill.
 #include "pa_common.cuh"
 #include "pa_kernels.cuh"
 

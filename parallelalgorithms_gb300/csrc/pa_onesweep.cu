@@ -14,21 +14,22 @@
 //      every tile a CTA waits on in step 5 is owned by a CTA already running);
 //   2. bulk-copy the tile global -> shared with the TMA engine, completing on
 //      an mbarrier (plain loads for the <16-byte ragged end, or when a buffer
-//      is not 16-byte aligned); a partial tile is padded with all-ones keys,
-//      which sort after every real key;
-//   3. sort the tile by the 8-bit digit in shared memory as two stable 4-bit
-//      counting passes (low nibble, then high nibble).  Each thread owns ITEMS
-//      consecutive keys, so (thread, item) order is input order; per-thread
-//      counters live in shared memory at [nibble][thread], one bank per
-//      thread, so counting is conflict-free and needs no warp-wide matching;
-//      a block-wide exclusive scan of the counters gives each key its
-//      position;
-//   4. bin counts of the tile from the run boundaries of the sorted tile;
-//      publish them (AGGREGATE, or INCLUSIVE for tile 0);
+//      is not 16-byte aligned);
+//   3. rank every key within the tile by its 8-bit digit (stable).  Default:
+//      warp multisplit (pa_onesweep_tile.cuh, onesweep_tile_ms_body) -- per
+//      item, the lanes holding the same digit are found by ballots or by a
+//      shared-memory atomic OR, one of them bumps the warp's counter for the
+//      digit; the warps' counters are scanned into the tile's bin offsets.
+//      Alternative (PA_ONESWEEP_RANK=counting): two stable 4-bit counting
+//      passes over the tile with per-thread counters (onesweep_tile);
+//   4. publish the tile's bin counts (AGGREGATE, or INCLUSIVE for tile 0);
 //   5. per bin, walk back over earlier tiles' words, four tiles per round
 //      trip, until an INCLUSIVE one; publish INCLUSIVE;
-//   6. write the sorted tile out: consecutive threads write consecutive keys
-//      of a bin to consecutive addresses.
+//   6. stage the keys at their in-tile sorted position in shared memory and
+//      write them out: consecutive threads write consecutive keys of a bin to
+//      consecutive addresses.
+// Small inputs (at most small_sort_max_keys) are sorted whole by one CTA in
+// shared memory instead (small_sort_kernel).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>

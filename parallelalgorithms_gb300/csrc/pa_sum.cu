@@ -1,7 +1,9 @@
 // Exact 64-bit sum: GPU form of SumParallelNonRecursive / SumParallel
 // (SumParallel.h:162-307).  The reference cuts the array into 16K-element
-// tasks and adds the per-task sums serially; here each thread accumulates
-// 16-byte vectors into a 64-bit register, warps and CTAs reduce with shuffles,
+// tasks and adds the per-task sums serially; here the array streams through
+// shared memory by bulk copies (pa_bulkstream.cuh), each consumer thread
+// accumulates 16-byte vectors into a 64-bit register, warps and CTAs reduce
+// with shuffles,
 // each CTA writes one partial, and the last CTA to finish (ticket) adds the
 // partials in CTA order.  Integer addition modulo 2^64 is associative, so
 // the result equals the reference's bit for bit whatever the split.
