@@ -19,10 +19,12 @@
 #include <string>
 #include <tuple>
 #include <utility>
+#include <vector>
 
 #include "pa_gpu.h"
 #include "pa_common.cuh"
 #include "pa_kernels.cuh"
+#include "pa_segmented.cuh"
 
 namespace pa {
 
@@ -82,7 +84,8 @@ struct Workspace {
   // pipelined host-buffer sort (created on first use)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t pipe_ev[kPipeChunks + kPipeGroups + 2] = {};
-  unsigned long long* pipe_host = nullptr;  // pinned: per-chunk counts, per-group pieces
+  void* pipe_host = nullptr;                // pinned staging of the pipelined sort (grow-only)
+  size_t pipe_host_cap = 0;
 };
 
 std::mutex g_mu;
@@ -217,33 +220,54 @@ bool fault_pipeline_oom() {
   return v;
 }
 
+// The workspace's page-locked staging block, grown to at least `bytes`
+// (growing frees the old block, which waits for the device: only between
+// calls, before any copy from it is queued).  nullptr if it cannot grow.
+void* pipe_pinned(Workspace* ws, size_t bytes) {
+  if (bytes <= ws->pipe_host_cap) return ws->pipe_host;
+  if (ws->pipe_host) cudaFreeHost(ws->pipe_host);
+  ws->pipe_host = nullptr;
+  ws->pipe_host_cap = 0;
+  const size_t cap = std::max(bytes + bytes / 4, (size_t)1 << 20);
+  if (cudaMallocHost(&ws->pipe_host, cap) != cudaSuccess) {
+    cudaGetLastError();
+    ws->pipe_host = nullptr;
+    return nullptr;
+  }
+  ws->pipe_host_cap = cap;
+  return ws->pipe_host;
+}
+
 int pipelined_host_sort(Workspace* ws, cudaStream_t stream, void* keys, size_t n, int kb) {
-  static_assert(kPipeChunks <= 16, "a group gathers at most 16 pieces");
   if (fault_pipeline_oom()) return set_error(PA_ERR_OOM, "injected allocation failure (PA_FAULT_PIPELINE_OOM)");
-  constexpr size_t kHostWords = (size_t)kPipeChunks * 256 + (size_t)kPipeGroups * kPipeChunks * 2;
   if (!ws->copy_stream) PA_CUDA(cudaStreamCreateWithFlags(&ws->copy_stream, cudaStreamNonBlocking));
   for (auto& e : ws->pipe_ev)
     if (!e) PA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  if (!ws->pipe_host) PA_CUDA(cudaMallocHost(&ws->pipe_host, kHostWords * 8));
   const uint32_t top_shift = 8u * (uint32_t)kb - 8u;
   const size_t chunk = ((n + kPipeChunks - 1) / kPipeChunks + 3) & ~(size_t)3;
   const size_t ctiles = ceil_div(chunk, onesweep_tile_keys(kb, false));
   const size_t sb = onesweep_status_bytes(chunk);
-  char *d_keys = nullptr, *d_tmp = nullptr, *d_gs = nullptr, *status = nullptr, *gscratch = nullptr;
-  unsigned long long *counts = nullptr, *bin_start = nullptr, *pieces = nullptr;
+  // 32-bit groups are sorted bucket by bucket by the batched kernel (three
+  // passes: a bucket's top byte is constant); its plan block is bounded by
+  // n / 2 bytes of look-back words plus tables.
+  const size_t plan_cap = kb == 4 ? n / 2 + ((size_t)8 << 20) : 0;
+  char *d_keys = nullptr, *d_tmp = nullptr, *d_gs = nullptr, *status = nullptr, *gscratch = nullptr, *plan_dev = nullptr;
+  unsigned long long *counts = nullptr, *bin_start = nullptr, *runs = nullptr;
   uint32_t* tile_ctr = nullptr;
   SortCtrl* ctrl = nullptr;
+  constexpr size_t kMaxRuns = (size_t)256 * kPipeChunks;  // every (bucket, chunk) piece
   auto layout = [&](Carve& c) {
     d_keys = c.take<char>(n * kb);  // input chunks; later the gathered groups
     d_tmp = c.take<char>(n * kb);   // chunks split into buckets
-    d_gs = c.take<char>(n * kb);    // the group sorts' scratch
+    d_gs = c.take<char>(n * kb);    // the group sorts' scratch (and 3-pass results)
     counts = c.take<unsigned long long>((size_t)kPipeChunks * 256);
     tile_ctr = c.take<uint32_t>(kPipeChunks);
     status = c.take<char>((size_t)kPipeChunks * ctiles * 256 * sb);
     bin_start = c.take<unsigned long long>((size_t)kPipeChunks * 256);
     ctrl = c.take<SortCtrl>(kPipeChunks);
-    pieces = c.take<unsigned long long>((size_t)kPipeGroups * kPipeChunks * 2);
+    runs = c.take<unsigned long long>(kMaxRuns * 3);
     gscratch = c.take<char>(sort_scratch_bytes(n, kb, false));
+    plan_dev = c.take<char>(plan_cap);
   };
   Carve m{nullptr};
   layout(m);
@@ -286,11 +310,16 @@ int pipelined_host_sort(Workspace* ws, cudaStream_t stream, void* keys, size_t n
     PA_CUDA(launch_onesweep_pass(a, kb, false, stream));
   }
   clo[nc] = n;
-  unsigned long long* hc = ws->pipe_host;  // [chunks][256] counts
-  PA_CUDA(cudaMemcpyAsync(hc, counts, (size_t)nc * 256 * 8, cudaMemcpyDeviceToHost, stream));
-  PA_CUDA(cudaStreamSynchronize(stream));
+  std::vector<unsigned long long> hc((size_t)nc * 256);  // [chunks][256] counts
+  {
+    unsigned long long* stage = static_cast<unsigned long long*>(pipe_pinned(ws, (size_t)nc * 256 * 8));
+    if (!stage) return set_error(PA_ERR_OOM, "page-locked staging for the pipelined sort");
+    PA_CUDA(cudaMemcpyAsync(stage, counts, (size_t)nc * 256 * 8, cudaMemcpyDeviceToHost, stream));
+    PA_CUDA(cudaStreamSynchronize(stream));
+    std::memcpy(hc.data(), stage, hc.size() * 8);
+  }
 
-  // 2. groups of whole buckets; each group's pieces, one per chunk
+  // 2. groups of whole buckets; each group's runs, bucket by bucket, one per chunk
   unsigned long long total[257] = {};
   for (int b = 0; b < 256; ++b)
     for (int c = 0; c < nc; ++c) total[b + 1] += hc[(size_t)c * 256 + b];
@@ -304,30 +333,74 @@ int pipelined_host_sort(Workspace* ws, cudaStream_t stream, void* keys, size_t n
   for (int b = 1; b < 256 && ng < want_groups - 1; ++b)
     if (total[b] - total[gb[ng]] >= share && total[b] < n) gb[++ng] = b;
   gb[++ng] = 256;
-  unsigned long long* hp = hc + (size_t)kPipeChunks * 256;  // [groups][chunks] (offset, count)
+  // bucket b of chunk c starts at clo[c] + (its counts of buckets < b) in d_tmp
+  std::vector<unsigned long long> local((size_t)nc * 257);
   for (int c = 0; c < nc; ++c) {
-    unsigned long long start = 0;  // the chunk's bucket starts, walked group by group
-    int b = 0;
-    for (int g = 0; g < ng; ++g) {
-      const unsigned long long gstart = start;
-      for (; b < gb[g + 1]; ++b) start += hc[(size_t)c * 256 + b];
-      hp[((size_t)g * kPipeChunks + c) * 2] = clo[c] + gstart;
-      hp[((size_t)g * kPipeChunks + c) * 2 + 1] = start - gstart;
-    }
+    local[(size_t)c * 257] = 0;
+    for (int b = 0; b < 256; ++b) local[(size_t)c * 257 + b + 1] = local[(size_t)c * 257 + b] + hc[(size_t)c * 256 + b];
   }
-  PA_CUDA(cudaMemcpyAsync(pieces, hp, (size_t)ng * kPipeChunks * 2 * 8, cudaMemcpyHostToDevice, stream));
+  std::vector<unsigned long long> run_tab;  // (src, len, dst) triples, group by group
+  std::vector<size_t> run_first(ng + 1), run_max(ng, 0);
+  for (int g = 0; g < ng; ++g) {
+    run_first[g] = run_tab.size() / 3;
+    const unsigned long long g0 = total[gb[g]];
+    for (int b = gb[g]; b < gb[g + 1]; ++b)
+      for (int c = 0; c < nc; ++c) {
+        const unsigned long long len = hc[(size_t)c * 256 + b];
+        if (!len) continue;
+        unsigned long long dst = total[b] - g0;  // within the group, bucket b, then chunk order
+        for (int c2 = 0; c2 < c; ++c2) dst += hc[(size_t)c2 * 256 + b];
+        run_tab.insert(run_tab.end(), {clo[c] + local[(size_t)c * 257 + b], len, dst});
+        run_max[g] = std::max<size_t>(run_max[g], (size_t)len);
+      }
+  }
+  run_first[ng] = run_tab.size() / 3;
+  // per-group batched plans (32-bit keys): buckets as segments, three passes
+  std::vector<seg::HostPlan> plans(kb == 4 ? ng : 0);
+  std::vector<size_t> image_off(ng + 1, 0);
+  bool batched = kb == 4;
+  for (int g = 0; g < ng && batched; ++g) {
+    std::vector<uint64_t> off(gb[g + 1] - gb[g] + 1);
+    for (int b = gb[g]; b <= gb[g + 1]; ++b) off[b - gb[g]] = total[b] - total[gb[g]];
+    pa_segsort_config cfg{};
+    cfg.small_cutoff = 4096;
+    cfg.tile_keys = 8192;
+    if (seg::build_host_plan(off.data(), off.size() - 1, &cfg, &plans[g], 3) != PA_OK || plans[g].bytes > plan_cap)
+      batched = false;  // (a bucket past the batched sort's limits) the plain sort takes the groups
+    image_off[g + 1] = image_off[g] + ((batched ? seg::plan_image_bytes(plans[g]) : 0) + 255) / 256 * 256;
+  }
+  if (!batched) std::fill(image_off.begin(), image_off.end(), 0);
+  const size_t runs_bytes = run_tab.size() * 8;
+  const size_t images_at = (runs_bytes + 255) / 256 * 256;  // the plan images follow the run table
+  char* stage = static_cast<char*>(pipe_pinned(ws, images_at + image_off[ng]));
+  if (!stage) return set_error(PA_ERR_OOM, "page-locked staging for the pipelined sort");
+  std::memcpy(stage, run_tab.data(), runs_bytes);
+  PA_CUDA(cudaMemcpyAsync(runs, stage, runs_bytes, cudaMemcpyHostToDevice, stream));
+  char* images = stage + images_at;
 
   // 3. per group: gather, sort, copy out while the next group runs
   for (int g = 0; g < ng; ++g) {
     const size_t lo = (size_t)total[gb[g]], len = (size_t)(total[gb[g + 1]] - total[gb[g]]);
     if (len == 0) continue;
-    PA_CUDA(launch_gather_pieces(d_tmp, d_keys + lo * kb, pieces + (size_t)g * kPipeChunks * 2, nc, len, kb, stream));
-    SortScratch sc{};
-    sort_scratch_layout(gscratch, len, kb, false, &sc);
-    PA_CUDA(enqueue_sort(sc, d_keys + lo * kb, d_gs + lo * kb, nullptr, nullptr, len, kb, false, ws->err, stream));
+    PA_CUDA(launch_gather_runs(d_tmp, d_keys + lo * kb, runs + run_first[g] * 3, run_first[g + 1] - run_first[g],
+                               run_max[g], kb, stream));
+    char* result = d_keys + lo * kb;
+    if (batched) {
+      seg::HostPlan& hp = plans[g];
+      PA_CUDA(seg::upload_plan(hp, plan_dev, stream, images + image_off[g]));
+      seg::PlanDev pd = seg::device_view(hp, plan_dev, reinterpret_cast<uint32_t*>(d_keys + lo * kb),
+                                         reinterpret_cast<uint32_t*>(d_gs + lo * kb));
+      pd.err = ws->err;
+      PA_CUDA(seg::launch_plan(hp, pd, plan_dev, seg::plan_grid(hp), stream));
+      result = reinterpret_cast<char*>(seg::result_buffer(pd));
+    } else {
+      SortScratch sc{};
+      sort_scratch_layout(gscratch, len, kb, false, &sc);
+      PA_CUDA(enqueue_sort(sc, d_keys + lo * kb, d_gs + lo * kb, nullptr, nullptr, len, kb, false, ws->err, stream));
+    }
     PA_CUDA(cudaEventRecord(ev[1 + kPipeChunks + g], stream));
     PA_CUDA(cudaStreamWaitEvent(cs, ev[1 + kPipeChunks + g], 0));
-    PA_CUDA(cudaMemcpyAsync(h + lo * kb, d_keys + lo * kb, len * kb, cudaMemcpyDeviceToHost, cs));
+    PA_CUDA(cudaMemcpyAsync(h + lo * kb, result, len * kb, cudaMemcpyDeviceToHost, cs));
   }
   PA_CUDA(cudaEventRecord(ev[kPipeChunks + kPipeGroups + 1], cs));
   PA_CUDA(cudaStreamWaitEvent(stream, ev[kPipeChunks + kPipeGroups + 1], 0));

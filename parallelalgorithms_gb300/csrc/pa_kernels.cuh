@@ -109,11 +109,12 @@ cudaError_t launch_onesweep_pass(const OnesweepArgs& a, int key_bytes, bool has_
 size_t small_sort_max_keys(int key_bytes, bool has_vals);
 cudaError_t launch_small_sort(void* keys, uint32_t* vals, size_t n, int key_bytes, bool is_float, cudaStream_t stream);
 
-// dst[0, total) = the concatenation of `npieces` runs of src, piece i being
-// src[pieces[2i], pieces[2i] + pieces[2i + 1]) (element offsets and counts;
-// npieces <= 16).  key_bytes 4 or 8.
-cudaError_t launch_gather_pieces(const void* src, void* dst, const unsigned long long* pieces, int npieces,
-                                 size_t total, int key_bytes, cudaStream_t stream);
+// Copies `nruns` (at most 65535) runs of elements: run r moves
+// src[runs[3r], +runs[3r + 1]) to dst[runs[3r + 2], ...) (element offsets
+// and counts; runs in device memory; max_run: the longest run, for the grid).
+// key_bytes 4 or 8.
+cudaError_t launch_gather_runs(const void* src, void* dst, const unsigned long long* runs, size_t nruns,
+                               size_t max_run, int key_bytes, cudaStream_t stream);
 
 // Copies the result back into the caller's buffers when the executed passes
 // left it in the scratch buffers (device-side decision from SortCtrl).

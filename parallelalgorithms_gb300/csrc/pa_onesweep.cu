@@ -141,20 +141,19 @@ __global__ void final_copy_kernel(K* keys_a, const K* keys_b, uint32_t* vals_a, 
   }
 }
 
-// One grid row per piece: the piece's elements go to their place in dst with
-// 16-byte vector stores (the loads are plain and coalesced: a warp reads
-// consecutive elements); the few elements before dst's first 16-byte
-// boundary and after its last one are copied singly.
+// One grid row per run: run r copies src[runs[3r], +runs[3r+1]) to
+// dst[runs[3r+2], ...) with 16-byte vector stores (the loads are plain and
+// coalesced: a warp reads consecutive elements); the few elements before the
+// destination's first 16-byte boundary and after its last one are copied
+// singly.
 template <typename K>
-__global__ void gather_pieces_kernel(const K* __restrict__ src, K* __restrict__ dst,
-                                     const unsigned long long* __restrict__ pieces, int npieces) {
+__global__ void gather_runs_kernel(const K* __restrict__ src, K* __restrict__ dst,
+                                   const unsigned long long* __restrict__ runs) {
   constexpr uint32_t V = 16 / sizeof(K);
-  const int p = blockIdx.y;
-  unsigned long long d0 = 0;  // where the piece starts in dst
-  for (int q = 0; q < p; ++q) d0 += pieces[2 * q + 1];
-  const K* s = src + pieces[2 * p];
-  const size_t len = (size_t)pieces[2 * p + 1];
-  K* d = dst + d0;
+  const size_t r = blockIdx.y;
+  const K* s = src + runs[3 * r];
+  const size_t len = (size_t)runs[3 * r + 1];
+  K* d = dst + runs[3 * r + 2];
   size_t head = ((16u - (reinterpret_cast<uintptr_t>(d) & 15u)) & 15u) / sizeof(K);
   if (head > len) head = len;
   const size_t nvec = (len - head) / V;
@@ -301,23 +300,21 @@ cudaError_t launch_small_sort(void* keys, uint32_t* vals, size_t n, int key_byte
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_gather_pieces(const void* src, void* dst, const unsigned long long* pieces, int npieces,
-                                 size_t total, int key_bytes, cudaStream_t stream) {
-  if (total == 0) return cudaSuccess;
-  if (npieces < 1 || npieces > 16) return cudaErrorInvalidValue;
+cudaError_t launch_gather_runs(const void* src, void* dst, const unsigned long long* runs, size_t nruns,
+                               size_t max_run, int key_bytes, cudaStream_t stream) {
+  if (nruns == 0 || max_run == 0) return cudaSuccess;
+  if (nruns > 65535) return cudaErrorInvalidValue;
   const int block = 256;
-  // each piece gets about total / npieces elements; a CTA moves 16 vectors per thread
-  const size_t per_piece = ceil_div(total, (size_t)npieces);
   const size_t vec = 16 / (size_t)key_bytes;
-  const unsigned gx = (unsigned)max((size_t)1, min(ceil_div(per_piece, (size_t)block * vec * 16),
+  const unsigned gx = (unsigned)max((size_t)1, min(ceil_div(max_run, (size_t)block * vec * 8),
                                                    (size_t)device_info().sm_count * 2));
-  const dim3 grid(gx, (unsigned)npieces);
+  const dim3 grid(gx, (unsigned)nruns);
   if (key_bytes == 4)
-    gather_pieces_kernel<uint32_t><<<grid, block, 0, stream>>>(static_cast<const uint32_t*>(src),
-                                                               static_cast<uint32_t*>(dst), pieces, npieces);
+    gather_runs_kernel<uint32_t><<<grid, block, 0, stream>>>(static_cast<const uint32_t*>(src),
+                                                             static_cast<uint32_t*>(dst), runs);
   else if (key_bytes == 8)
-    gather_pieces_kernel<unsigned long long><<<grid, block, 0, stream>>>(
-        static_cast<const unsigned long long*>(src), static_cast<unsigned long long*>(dst), pieces, npieces);
+    gather_runs_kernel<unsigned long long><<<grid, block, 0, stream>>>(
+        static_cast<const unsigned long long*>(src), static_cast<unsigned long long*>(dst), runs);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();

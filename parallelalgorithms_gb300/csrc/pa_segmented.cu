@@ -116,7 +116,8 @@ __device__ __forceinline__ void small_item(const PlanDev& P, const Item& it, uns
   uint32_t* s_warp = reinterpret_cast<uint32_t*>(smem + GS::kWarpTotOff);
   const unsigned long long base = P.seg_off[it.seg];
   const uint32_t len = (uint32_t)(P.seg_off[it.seg + 1] - base);
-  uint32_t* keys = P.keys + base;
+  const uint32_t* keys = P.keys + base;
+  uint32_t* out = result_buffer(P) + base;
   for (uint32_t i = threadIdx.x; i < TILE; i += kBlock) s_keys[i] = i < len ? keys[i] : 0xFFFFFFFFu;
   __syncthreads();
   uint32_t k[SMALL_ITEMS];
@@ -126,7 +127,7 @@ __device__ __forceinline__ void small_item(const PlanDev& P, const Item& it, uns
     load_run<uint32_t, false, SMALL_ITEMS>(k, v, s_keys, nullptr);
     nibble_pass<uint32_t, false, kBlock, SMALL_ITEMS>(k, v, sh, s_keys, nullptr, s_cnt, s_warp);
   }
-  for (uint32_t i = threadIdx.x; i < len; i += kBlock) keys[i] = s_keys[i];
+  for (uint32_t i = threadIdx.x; i < len; i += kBlock) out[i] = s_keys[i];
 }
 
 template <int PASS_ITEMS, int SMALL_ITEMS>
@@ -214,7 +215,9 @@ bool pick_kernel(int tile_keys, int small_cutoff, KernelChoice* out) {
 }
 
 // ---- host-side planning --------------------------------------------------------
-int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segsort_config* cfg, HostPlan* hp) {
+int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segsort_config* cfg, HostPlan* hp,
+                    int passes) {
+  if (passes < 1 || passes > kPasses) return record_error(PA_ERR_ARG, "a batched plan runs 1 to 4 digit passes");
   pa_segsort_config c{};
   if (cfg) c = *cfg;
   for (int r : c.reserved)
@@ -234,6 +237,7 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
   }
   hp->cfg = c;
   hp->kc = kc;
+  hp->passes = (uint32_t)passes;
   hp->off.assign(off, off + num_segments + 1);
   hp->items.clear();
   hp->large.clear();
@@ -241,7 +245,7 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
   uint32_t total_tiles = 0;
   for (size_t i = 0; i < num_segments; ++i) {
     const uint64_t len = off[i + 1] - off[i];
-    if (len <= 1) continue;
+    if (len == 0 || (len == 1 && (passes % 2) == 0)) continue;  // (an odd pass count moves even single keys to tmp)
     if (len <= (uint64_t)kc.small_tile && len <= (uint64_t)c.small_cutoff) {
       small_ids.push_back((uint32_t)i);
     } else {
@@ -260,7 +264,7 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
                    [&](uint32_t a, uint32_t b) { return off[a + 1] - off[a] > off[b + 1] - off[b]; });
   auto& items = hp->items;
   size_t next_small = 0;
-  const size_t gaps = 1 + 1 + kPasses;  // after HIST, SCAN, and each pass but the last
+  const size_t gaps = 1 + 1 + (size_t)passes;  // after HIST, SCAN, and each pass but the last
   auto add_small = [&](size_t share_of) {
     const size_t upto = std::min(small_ids.size(), (small_ids.size() * share_of + gaps - 1) / gaps);
     for (; next_small < upto; ++next_small) items.push_back({ITEM_SMALL, 0, small_ids[next_small], 0});
@@ -271,7 +275,7 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
   add_small(1);
   for (uint32_t l = 0; l < nlarge; ++l) items.push_back({ITEM_SCAN, 0, l, 0});
   add_small(2);
-  for (uint32_t p = 0; p < (uint32_t)kPasses; ++p) {
+  for (uint32_t p = 0; p < (uint32_t)passes; ++p) {
     for (uint32_t l = 0; l < nlarge; ++l)
       for (uint32_t t = 0; t < hp->large[l].tiles; ++t) items.push_back({ITEM_PASS, p, l, t});
     add_small(3 + p);
@@ -306,6 +310,7 @@ PlanDev device_view(const HostPlan& hp, char* dev, uint32_t* keys, uint32_t* tmp
   PlanDev d{};
   d.keys = keys;
   d.tmp = tmp;
+  d.passes = hp.passes;
   d.items = reinterpret_cast<const Item*>(dev + hp.o_items);
   d.num_items = (uint32_t)hp.items.size();
   d.total_tiles = hp.total_tiles;

@@ -41,6 +41,8 @@ struct LargeSeg {
 struct PlanDev {
   uint32_t* keys;
   uint32_t* tmp;
+  uint32_t passes;                 // low digits sorted by the large segments' passes (4: all);
+                                   // results end in keys for an even count, in tmp for an odd one
   const Item* items;
   uint32_t num_items;
   uint32_t total_tiles;
@@ -73,14 +75,22 @@ struct HostPlan {
   std::vector<LargeSeg> large;
   std::vector<uint64_t> off;
   uint32_t total_tiles = 0, num_small = 0, num_large = 0;
+  uint32_t passes = kPasses;  // digit passes of the large segments (3: every segment's top byte is constant)
   size_t o_items = 0, o_off = 0, o_large = 0, o_bins = 0, o_err = 0, o_head = 0, o_done = 0, o_hist = 0,
          o_status = 0, bytes = 0;
 };
 
 // Validates the offsets and plans the queue and the device block layout.
-int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segsort_config* cfg, HostPlan* hp);
+// `passes` < 4 sorts large segments by their low `passes` bytes only (for
+// segments whose higher bytes are constant); results then end in tmp when
+// `passes` is odd (result_buffer).
+int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segsort_config* cfg, HostPlan* hp,
+                    int passes = kPasses);
 // Pointers of a device block laid out by `hp` (keys / tmp: the batch's keys).
 PlanDev device_view(const HostPlan& hp, char* dev, uint32_t* keys, uint32_t* tmp);
+// Where a run of `pd` leaves the sorted keys: keys after an even number of
+// passes, tmp after an odd one.
+__host__ __device__ inline uint32_t* result_buffer(const PlanDev& pd) { return (pd.passes & 1u) ? pd.tmp : pd.keys; }
 // Copies the queue, offsets and segment table into the block; clears its error word.
 // With `pinned_staging` (page-locked, at least plan_image_bytes(hp) bytes, left
 // untouched by the caller until the copy has run) the three tables go up in
