@@ -1,6 +1,5 @@
 // Streaming a contiguous byte range through shared memory with bulk copies
-// (the TMA engine's non-tensor form), for the read-once kernels (sum, the
-// filtering steps of radix select).
+// (the TMA engine's non-tensor form), for the read-once sum kernel.
 //
 // A CTA of CONSUMERS + 32 threads owns the chunks blockIdx.x, blockIdx.x +
 // gridDim.x, ... of the range (CHUNK bytes each, the last one possibly

@@ -3,59 +3,76 @@
 // GPU form of RadixSelectiontNonRecursiveInner (RadixSelect.h:83-129).  The
 // reference narrows MSD digit by digit: count the digit over the current
 // range (HistogramOneComponentOpt), find the bin holding k, move that bin's
-// keys together (MoveOutsideOfKthBinIn, :36-55), recurse into the bin.
-// Here nothing is moved in the input:
-//   step 0   every digit's counts over all keys come from one read by the
-//            one-read histogram kernel (digit_counts_kernel); a one-CTA pick
-//            finds the top digit's bin holding k;
-//   step s   while every key still shares the prefix found so far (one bin
-//            held them all), digit s's counts over all keys are the ones
-//            needed and no key is read; otherwise every key whose decided
-//            high digits equal the prefix is counted on digit s (lane-banked
-//            shared counters, 16-byte loads) and the last CTA of the step
-//            (ticket) picks the bin.
-// The first filtering step also copies the keys sharing the prefix into a
-// candidate buffer when they fit it, and later steps read only that buffer.
-// All state lives on the device, so the host enqueues key_bits / 8 + 2
-// launches and never waits between them.
-#include "pa_bulkstream.cuh"
+// keys together (MoveOutsideOfKthBinIn, :36-55), recurse into the bin.  The
+// result is the same order statistic; here the input is read once in the
+// usual case and never moved:
+//   sample   one CTA takes kSample keys at even strides and finds, by the
+//            same MSD digit narrowing in shared memory, the sample's keys
+//            `lo` and `hi` a few standard deviations below and above rank k
+//            (the extreme ranks give the key type's minimum / maximum);
+//   range    one streaming read of the input counts the keys below lo and
+//            equal to lo and to hi and copies the keys strictly between
+//            them (the candidates) to a buffer, branch-free per key; the
+//            last CTA (ticket) then either has the answer (lo or hi), or
+//            continues with rank k among the candidates (the first step
+//            counts their top digit), or (rank k outside the bracket, or the
+//            candidates overflowed: an unrepresentative sample) restarts the
+//            plain digit-by-digit narrowing over the whole input;
+//   step s   the digit below the decided prefix is counted over the keys of
+//            the current source (input or a candidate buffer) that share
+//            the prefix (lane-banked shared counters), and the last CTA
+//            picks the bin.  A step whose digit is already decided (or
+//            whose answer is already written) returns at once.
+// A step may copy the keys sharing the prefix into the next candidate
+// buffer (input -> buffer A -> buffer B) when they fit it, and later steps
+// read only that buffer.  All state lives on the device, so the host
+// enqueues key_bits / 8 + 3 launches and never waits between them.
+#include <cmath>
+
 #include "pa_common.cuh"
 #include "pa_kernels.cuh"
 
 namespace pa {
 
 struct SelectState {
-  unsigned long long hist_all[8][256];  // counts of every digit over all keys (step 0)
   unsigned long long hist[256];
-  unsigned long long prefix;       // decided high digits, right-aligned
-  unsigned long long k;            // rank sought among keys sharing prefix
-  unsigned long long count;        // keys sharing prefix
-  unsigned long long cand_n;       // keys in the candidate buffer
-  unsigned long long cand_fill;    // compaction cursor of the current step
+  unsigned long long prefix;        // decided high digits, right-aligned
+  unsigned long long k;             // rank sought among the current source's keys sharing prefix
+  unsigned long long count;         // keys sharing prefix
+  unsigned long long cand_n[2];     // keys in candidate buffer A / B
+  unsigned long long cand_fill;     // compaction cursor of the current step
+  unsigned long long lo, hi;        // the sample's bracket around rank k
+  unsigned long long below, eq_lo, eq_hi;  // range pass: keys < lo, == lo, == hi (hi != lo)
   uint32_t prefix_bits;
-  uint32_t src;                    // 0: the input array, 1: candidate buffer
+  uint32_t src;                     // 0: the input array, 1: buffer A, 2: buffer B
   uint32_t ticket;
-  uint32_t all_digits;             // hist_all holds every digit (else only the top one)
+  uint32_t done;                    // the result is written
+  uint32_t overflow;                // the range pass's candidates did not fit buffer A
 };
 
 namespace {
 
-// A filtering step streams its source through shared memory by bulk copies
-// (three 16 KB stages per CTA, two CTAs per SM, 512 consumer threads each
-// taking two vectors of every chunk).
-constexpr int kStages = 3;
-constexpr int kChunk = 16 * 1024;
-constexpr int kConsumers = 512;
-constexpr int kPerThread = kChunk / 16 / kConsumers;
-static_assert(kPerThread * kConsumers * 16 == kChunk, "a chunk splits evenly over the consumers");
-using Ring = BulkRing<kStages, kChunk, kConsumers>;
-constexpr int kSelBlock = Ring::kThreads;
-constexpr int kSelLanes = 32;  // lane copies of each shared counter
-// Candidates a CTA gathers in shared memory before one global reservation
-// (12 KB, so that counters and buffer stay under 48 KB of static shared
-// memory).
+// A streaming kernel runs one CTA of 1024 threads per SM; each thread keeps
+// kUnroll 16-byte loads in flight per grid-strided round.
+constexpr int kSelBlock = 1024;
+constexpr int kSelWarps = kSelBlock / 32;
+constexpr int kUnroll = 4;
+constexpr int kSelLanes = 16;  // lane copies of each shared counter
+// Candidates are staged per warp in shared memory (a segment holding one
+// round of the warp, so that one visit always fits after a flush) and leave
+// with one global reservation per segment.
+constexpr int kSegBytes = 32 * kUnroll * 16;
 template <typename K>
-constexpr int kCandBuf = 12 * 1024 / (int)sizeof(K);
+constexpr uint32_t kSegKeys = (uint32_t)(kSegBytes / sizeof(K));
+constexpr size_t kStreamSmem = (size_t)kSelWarps * kSegBytes;
+// Sample size and bracket width: the sample's rank of the k-th key has
+// standard deviation sqrt(S p (1 - p)) (p = k / n); the bracket spans five
+// of them on each side, so about 5.5 % of a uniform input lies inside it
+// for the median and the sample misses rank k with probability ~1e-6.
+constexpr int kSampleLog2 = 13;
+constexpr int kSample = 1 << kSampleLog2;
+constexpr int kSampleThreads = 1024;
+constexpr double kBracketSigmas = 5.0;
 
 template <typename K>
 __device__ __forceinline__ bool matches(K key, unsigned long long prefix, uint32_t prefix_bits) {
@@ -67,12 +84,18 @@ __device__ __forceinline__ bool matches(K key, unsigned long long prefix, uint32
 // Picks the bin of h (256 complete counts of the next digit over the keys
 // sharing the prefix) holding rank st->k and narrows the state to it (called
 // by every thread of one CTA of at least 256 threads).  `compacted`: this
-// step filled the candidate buffer.
+// step filled the next candidate buffer.
 template <typename K>
 __device__ void pick_bin(SelectState* st, const unsigned long long* h, bool compacted, K* out) {
   constexpr uint32_t W = 8u * sizeof(K);
   __shared__ unsigned long long s_tot[8];
   const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+  // Every thread reads the state it tests before the barrier below, and the
+  // one thread whose bin holds rank k writes it only after that barrier: a
+  // thread reading st->k after the update would see the narrowed rank and
+  // could wrongly match a lower bin as well.
+  const unsigned long long k = st->k, prefix0 = st->prefix;
+  const uint32_t bits0 = st->prefix_bits, src0 = st->src;
   const unsigned long long c = t < 256 ? ld_relaxed_gpu(&h[t]) : 0ull;
   unsigned long long incl = c;  // inclusive scan of the 256 counts
 #pragma unroll
@@ -86,19 +109,21 @@ __device__ void pick_bin(SelectState* st, const unsigned long long* h, bool comp
     unsigned long long before = 0;
     for (uint32_t w = 0; w < warp; ++w) before += s_tot[w];
     const unsigned long long excl = before + incl - c;
-    const unsigned long long k = st->k;
     if (c != 0 && excl <= k && k < excl + c) {  // exactly one bin holds rank k
-      const unsigned long long prefix = (st->prefix << 8) | t;
+      const unsigned long long prefix = (prefix0 << 8) | t;
       st->prefix = prefix;
-      st->prefix_bits += 8;
+      st->prefix_bits = bits0 + 8;
       st->k = k - excl;
       st->count = c;
       if (compacted) {
-        st->src = 1;
-        st->cand_n = ld_relaxed_gpu(&st->cand_fill);  // filled by every CTA's atomics
+        st->cand_n[src0] = ld_relaxed_gpu(&st->cand_fill);  // filled by every CTA's atomics
+        st->src = src0 + 1;
       }
       st->cand_fill = 0;
-      if (st->prefix_bits == W) *out = (K)prefix;
+      if (bits0 + 8 == W) {
+        *out = (K)prefix;
+        st->done = 1;
+      }
     }
   }
   __syncthreads();
@@ -106,137 +131,250 @@ __device__ void pick_bin(SelectState* st, const unsigned long long* h, bool comp
   if (t == 0) st->ticket = 0;
 }
 
+// The bracket: kSample keys at even strides, and their order statistics at
+// the ranks kBracketSigmas standard deviations either side of rank k's
+// image, both found at once by MSD digit narrowing over the sample in
+// shared memory.
 template <typename K>
-__global__ void __launch_bounds__(256) select_pick_kernel(SelectState* st, K* out) {
+__global__ void __launch_bounds__(kSampleThreads) select_sample_kernel(const K* keys, size_t n, SelectState* st) {
   constexpr uint32_t W = 8u * sizeof(K);
-  pick_bin<K>(st, st->hist_all[W / 8 - 1], false, out);
+  extern __shared__ __align__(16) unsigned char sample_raw[];
+  K* s = reinterpret_cast<K*>(sample_raw);
+  __shared__ uint32_t s_h[2][256];
+  __shared__ unsigned long long s_pref[2], s_rank[2];
+  __shared__ bool s_lo_min, s_hi_max;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t ns = (uint32_t)(n < (size_t)kSample ? n : (size_t)kSample);
+  // key j of the sample sits at (j n + n / 2) / ns: a shift when ns is the
+  // full sample (a power of two), j itself when the input is smaller
+#pragma unroll
+  for (int q = 0; q < kSample / kSampleThreads; ++q) {  // independent loads, all in flight at once
+    const uint32_t j = tid + (uint32_t)q * kSampleThreads;
+    if (j < ns) s[j] = keys[ns == (uint32_t)kSample ? ((size_t)j * n + n / 2) >> kSampleLog2 : (size_t)j];
+  }
+  if (tid == 0) {
+    const double p = ((double)st->k + 0.5) / (double)n;
+    long long r = (long long)(p * (double)ns);
+    if (r > (long long)ns - 1) r = (long long)ns - 1;
+    const long long m = (long long)(kBracketSigmas * sqrt((double)ns * p * (1.0 - p))) + 2;
+    const long long r_lo = r > m ? r - m : 0;
+    const long long r_hi = r + m < (long long)ns - 1 ? r + m : (long long)ns - 1;
+    s_rank[0] = (unsigned long long)r_lo;
+    s_rank[1] = (unsigned long long)r_hi;
+    s_lo_min = r_lo == 0;  // no sample key below the bracket: open it down to the minimum
+    s_hi_max = r_hi == (long long)ns - 1;
+    s_pref[0] = s_pref[1] = 0;
+  }
+  uint32_t pbits = 0;
+  for (int d = (int)W / 8 - 1; d >= 0; --d) {
+    const uint32_t shift = 8u * (uint32_t)d;
+    for (uint32_t i = tid; i < 512u; i += kSampleThreads) (&s_h[0][0])[i] = 0;
+    __syncthreads();
+    const unsigned long long p0 = s_pref[0], p1 = s_pref[1];
+    for (uint32_t j = tid; j < ns; j += kSampleThreads) {
+      const K key = s[j];
+      const uint32_t dig = (uint32_t)(key >> shift) & 255u;
+      if (matches(key, p0, pbits)) atomicAdd(&s_h[0][dig], 1u);
+      if (matches(key, p1, pbits)) atomicAdd(&s_h[1][dig], 1u);
+    }
+    __syncthreads();
+    if (tid < 64) {  // warp t narrows target t; lane l owns bins [8l, 8l + 8)
+      const uint32_t t = tid >> 5, lane = tid & 31u;
+      uint32_t c[8], sum = 0;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        c[i] = s_h[t][8 * lane + i];
+        sum += c[i];
+      }
+      uint32_t incl = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+      }
+      const unsigned long long rk = s_rank[t];
+      const unsigned long long pref = s_pref[t];
+      __syncwarp();  // every lane has read the target before one lane narrows it
+      uint32_t acc = incl - sum;
+      if ((unsigned long long)acc <= rk && rk < (unsigned long long)incl) {
+        for (int i = 0; i < 8; ++i) {
+          if (rk < (unsigned long long)(acc + c[i])) {
+            s_pref[t] = (pref << 8) | (8u * lane + (uint32_t)i);
+            s_rank[t] = rk - acc;
+            break;
+          }
+          acc += c[i];
+        }
+      }
+    }
+    pbits += 8;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    st->lo = s_lo_min ? 0ull : s_pref[0];
+    st->hi = s_hi_max ? (unsigned long long)(K)~(K)0 : s_pref[1];
+  }
 }
 
-// One filtering step: counts digit `shift` of the keys sharing the prefix,
-// optionally copies them to the candidate buffer; the last CTA picks.
+// A consumer warp's candidate segment in shared memory: `fill` keys (the
+// same value in every lane).  seg_flush writes them to dst with one global
+// reservation (one past the capacity only raises st->overflow);
+// seg_append adds this thread's matched keys (kk[e] where bit e of mm is
+// set), flushing first when they would not fit.  Both are warp-collective.
 template <typename K>
-__global__ void __launch_bounds__(kSelBlock, 2) select_step_kernel(const K* keys, size_t n, K* cand, size_t cand_cap,
-                                                                   SelectState* st, uint32_t shift, K* out,
-                                                                   uint32_t* err) {
-  extern __shared__ __align__(128) unsigned char ring[];
-  constexpr int V = 16 / (int)sizeof(K);
+__device__ __forceinline__ void seg_flush(K* seg, uint32_t& fill, K* dst, size_t cap, SelectState* st) {
   constexpr uint32_t FULL = 0xFFFFFFFFu;
-  constexpr uint32_t CB = (uint32_t)kCandBuf<K>;
-  __shared__ uint32_t s_h[256 * kSelLanes];
-  __shared__ K s_cand[CB];
-  __shared__ uint32_t s_cn, s_valid;
-  __shared__ unsigned long long s_base;
-  __shared__ bool s_last;
-  for (uint32_t i = threadIdx.x; i < 256u * kSelLanes; i += kSelBlock) s_h[i] = 0;
-  if (threadIdx.x == 0) {
-    s_cn = 0;
-    s_valid = CB;
-  }
-
-  // The state read here changes only in the last CTA, after every CTA has
-  // taken its ticket.  When every key shares the prefix, digit `shift`'s
-  // counts over all keys (step 0) are the ones needed and nothing is read.
-  const bool all_share = st->all_digits && st->count == (unsigned long long)n;
-  const unsigned long long prefix = st->prefix;
-  const uint32_t prefix_bits = st->prefix_bits;
-  const uint32_t src = st->src;
-  // Compaction happens at most once (only while reading the input array),
-  // so it never overlaps its own source.
-  const bool compact = !all_share && src == 0 && st->count <= (unsigned long long)cand_cap;
-  const K* in = src ? cand : keys;
-  const size_t len = all_share ? 0 : src ? (size_t)st->cand_n : n;
-  __syncthreads();
-
+  if (fill == 0) return;
   const uint32_t lane = threadIdx.x & 31u;
-  uint32_t* my = s_h + lane;
-  auto count_key = [&](K key) { atomicAdd(my + (((uint32_t)(key >> shift) & 255u) * kSelLanes), 1u); };
-  // Warp-aggregated append of this thread's matched keys (kk where mm):
-  // into the CTA's shared buffer while it has room, else straight to the
-  // candidate buffer.  Shared reservations only grow, so the first one that
-  // does not fit marks the end of the valid shared entries (s_valid).
-  auto append = [&](const K* kk, const bool* mm, int nk) {
-    uint32_t cnt = 0;
-    for (int e = 0; e < nk; ++e) cnt += mm[e] ? 1u : 0u;
-    if (__ballot_sync(FULL, cnt != 0) == 0) return;
-    uint32_t incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t v = __shfl_up_sync(FULL, incl, o);
-      if (lane >= (uint32_t)o) incl += v;
-    }
-    const uint32_t total = __shfl_sync(FULL, incl, 31);
-    uint32_t pos = 0;
-    if (lane == 31) {
-      pos = atomicAdd(&s_cn, total);
-      if (pos + total > CB) atomicMin(&s_valid, pos);
-    }
-    pos = __shfl_sync(FULL, pos, 31);
-    if (pos + total <= CB) {
-      uint32_t at = pos + (incl - cnt);
-      for (int e = 0; e < nk; ++e)
-        if (mm[e]) s_cand[at++] = kk[e];
-      return;
-    }
-    unsigned long long base = 0;
-    if (lane == 31) base = atomicAdd(&st->cand_fill, (unsigned long long)total);
-    base = __shfl_sync(FULL, base, 31) + (incl - cnt);
-    for (int e = 0; e < nk; ++e)
-      if (mm[e]) cand[base++] = kk[e];
-  };
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(&st->cand_fill, (unsigned long long)fill);
+  base = __shfl_sync(FULL, base, 0);
+  __syncwarp();  // every lane's segment writes are visible
+  if (base + fill <= cap) {
+    for (uint32_t i = lane; i < fill; i += 32) dst[base + i] = seg[i];
+  } else if (lane == 0) {
+    st->overflow = 1;
+  }
+  __syncwarp();  // the segment is read out before it is refilled
+  fill = 0;
+}
 
-  // Split [0, len) into an unaligned head, whole 16-byte vectors and a tail;
-  // the vectors stream through the bulk-copy ring.
+template <typename K>
+__device__ __forceinline__ void seg_append(const K* kk, uint32_t mm, int nk, K* seg, uint32_t& fill, K* dst,
+                                           size_t cap, SelectState* st) {
+  constexpr uint32_t FULL = 0xFFFFFFFFu;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t cnt = __popc(mm);
+  if (__ballot_sync(FULL, cnt != 0) == 0) return;
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(FULL, incl, o);
+    if (lane >= (uint32_t)o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(FULL, incl, 31);
+  if (fill + total > kSegKeys<K>) seg_flush<K>(seg, fill, dst, cap, st);
+  uint32_t at = fill + incl - cnt;
+  for (int e = 0; e < nk; ++e)
+    if ((mm >> e) & 1u) seg[at++] = kk[e];
+  fill += total;
+}
+
+// Streams src[0, len) with 16-byte loads straight into registers, kUnroll
+// of them in flight per thread (vectors i, i + stride, ... of a grid-strided
+// round); visit(keys, valid, nk) is called by every thread once per round,
+// the same number of times on every lane, with bit e of `valid` set when key
+// e is present (a compile-time all-ones mask in the full rounds, so that the
+// masking costs nothing there), and once more per 32 keys by the first
+// CTA's first warp for the unaligned head and tail (one key per lane).
+// Called by all threads; ends with a barrier.
+template <typename K, typename F>
+__device__ __forceinline__ void stream_keys(const K* in, size_t len, F&& visit) {
+  constexpr int V = 16 / (int)sizeof(K);
   const uintptr_t addr = reinterpret_cast<uintptr_t>(in);
   size_t head = ((16u - (addr & 15u)) & 15u) / sizeof(K);
   if (head > len) head = len;
   const size_t nvec = (len - head) / V;
   const size_t tail_start = head + nvec * V;
-  bulk_stream<kStages, kChunk, kConsumers>(in + head, nvec * 16, ring, err, [&](const uint4* stq, uint32_t nv) {
-    // a full chunk is one round of kPerThread vectors per thread; a short last
-    // chunk masks the missing ones (same trip count on every lane)
-    K kk[kPerThread * V];
-    bool mm[kPerThread * V];
+  const uint4* vec = reinterpret_cast<const uint4*>(in + head);
+  const size_t stride = (size_t)gridDim.x * kSelBlock;
+  const size_t per_round = (size_t)kUnroll * stride;
+  const size_t full = nvec / per_round;  // rounds with every vector present
+  size_t i = (size_t)blockIdx.x * kSelBlock + threadIdx.x;
+  auto round = [&](bool masked) {
+    uint4 q[kUnroll];
+    uint32_t valid = 0xFFFFFFFFu;
 #pragma unroll
-    for (int u = 0; u < kPerThread; ++u) {
-      const uint32_t v = (uint32_t)u * kConsumers + threadIdx.x;
-      const bool in_range = v < nv;
-      const uint4 q = in_range ? stq[v] : make_uint4(0, 0, 0, 0);
-      const K* e = reinterpret_cast<const K*>(&q);
-#pragma unroll
-      for (int j = 0; j < V; ++j) {
-        kk[u * V + j] = e[j];
-        mm[u * V + j] = in_range && matches(e[j], prefix, prefix_bits);
-        if (mm[u * V + j]) count_key(e[j]);
+    for (int u = 0; u < kUnroll; ++u) {
+      const size_t j = i + (size_t)u * stride;
+      if (masked && j >= nvec) {
+        q[u] = make_uint4(0, 0, 0, 0);
+        valid &= ~(((1u << V) - 1u) << (u * V));
+      } else {
+        q[u] = ld_stream_v4(vec + j);
       }
     }
-    if (compact) append(kk, mm, kPerThread * V);
-  });
+    K kk[kUnroll * V];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const K* e = reinterpret_cast<const K*>(&q[u]);
+#pragma unroll
+      for (int j = 0; j < V; ++j) kk[u * V + j] = e[j];
+    }
+    if (masked)
+      visit(kk, valid, kUnroll * V);
+    else
+      visit(kk, 0xFFFFFFFFu, kUnroll * V);
+  };
+  for (size_t r = 0; r < full; ++r, i += per_round) round(false);
+  if (full * per_round < nvec) round(true);  // the last, partial round (the same on every thread)
   if (blockIdx.x == 0 && threadIdx.x < 32) {  // head and tail: fewer than 2 * V keys, one warp
     const size_t rest = head + (len - tail_start);
     for (size_t r0 = 0; r0 < rest; r0 += 32) {
       const size_t r = r0 + threadIdx.x;
       K key = 0;
-      bool m = false;
-      if (r < rest) {
-        key = in[r < head ? r : tail_start + (r - head)];
-        m = matches(key, prefix, prefix_bits);
-        if (m) count_key(key);
-      }
-      if (compact) append(&key, &m, 1);
+      const bool ok = r < rest;
+      if (ok) key = in[r < head ? r : tail_start + (r - head)];
+      visit(&key, ok ? 1u : 0u, 1);
     }
   }
   __syncthreads();
-  if (compact) {  // the CTA's shared candidates go out with one reservation
-    const uint32_t nv = min(s_cn, s_valid);
-    if (threadIdx.x == 0) s_base = nv ? atomicAdd(&st->cand_fill, (unsigned long long)nv) : 0ull;
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < nv; j += kSelBlock) cand[s_base + j] = s_cand[j];
-  }
-  // fold the lane copies (staggered so a warp's reads hit distinct banks)
+}
+
+// Folds the lane copies of the shared counters into st->hist (staggered so
+// a warp's reads hit distinct banks); CTAs that counted nothing skip it.
+// Called by all threads.
+__device__ __forceinline__ void fold_counts(const uint32_t* s_h, SelectState* st, bool counted) {
+  if (!__syncthreads_or(counted ? 1 : 0)) return;
   for (uint32_t b = threadIdx.x; b < 256u; b += kSelBlock) {
     uint32_t sum = 0;
     for (uint32_t j = 0; j < (uint32_t)kSelLanes; ++j) sum += s_h[b * kSelLanes + ((j + b) % kSelLanes)];
     if (sum) atomicAdd(&st->hist[b], (unsigned long long)sum);
+  }
+}
+
+// One read of the input against the bracket [lo, hi]; the last CTA decides
+// how the select continues.
+template <typename K>
+__global__ void __launch_bounds__(kSelBlock, 1) select_range_kernel(const K* keys, size_t n, K* cand_a, size_t cap_a,
+                                                                    SelectState* st, K* out) {
+  extern __shared__ __align__(128) unsigned char seg_smem[];
+  __shared__ uint32_t s_cnt[3];
+  __shared__ bool s_last;
+  if (threadIdx.x == 0) s_cnt[0] = s_cnt[1] = s_cnt[2] = 0;
+  const K lo = (K)st->lo, hi = (K)st->hi;
+  // strictly inside (lo, hi)  <=>  key - (lo + 1) < hi - lo - 1 (unsigned);
+  // nothing is inside when hi == lo
+  const K lo1 = (K)(lo + 1), w = hi > lo ? (K)(hi - lo - 1) : (K)0;
+  __syncthreads();
+  const uint32_t warp = threadIdx.x >> 5;
+  K* seg = reinterpret_cast<K*>(seg_smem) + (size_t)warp * kSegKeys<K>;
+  uint32_t fill = 0;
+  uint32_t below = 0, eq_lo = 0, eq_hi = 0;
+  // branch-free per key: three counts and a match bit (per-key branches
+  // or shared atomics here would cost more than the read itself)
+  stream_keys<K>(keys, n, [&](const K* kk, uint32_t valid, int nk) {
+    uint32_t mm = 0;
+#pragma unroll
+    for (int e = 0; e < nk; ++e) {
+      const K key = kk[e];
+      const bool v = (valid >> e) & 1u;
+      below += (v && key < lo) ? 1u : 0u;
+      eq_lo += (v && key == lo) ? 1u : 0u;
+      eq_hi += (v && key == hi) ? 1u : 0u;  // (discarded below when hi == lo)
+      mm |= (v && (K)(key - lo1) < w) ? (1u << e) : 0u;
+    }
+    seg_append<K>(kk, mm, nk, seg, fill, cand_a, cap_a, st);
+  });
+  seg_flush<K>(seg, fill, cand_a, cap_a, st);
+  if (below) atomicAdd(&s_cnt[0], below);
+  if (eq_lo) atomicAdd(&s_cnt[1], eq_lo);
+  if (eq_hi) atomicAdd(&s_cnt[2], eq_hi);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_cnt[0]) atomicAdd(&st->below, (unsigned long long)s_cnt[0]);
+    if (s_cnt[1]) atomicAdd(&st->eq_lo, (unsigned long long)s_cnt[1]);
+    if (s_cnt[2]) atomicAdd(&st->eq_hi, (unsigned long long)s_cnt[2]);
   }
   __threadfence();
   __syncthreads();
@@ -244,49 +382,144 @@ __global__ void __launch_bounds__(kSelBlock, 2) select_step_kernel(const K* keys
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  pick_bin<K>(st, all_share ? st->hist_all[shift / 8] : st->hist, compact, out);
+  if (threadIdx.x == 0) {
+    const unsigned long long k = st->k, b = ld_relaxed_gpu(&st->below), el = ld_relaxed_gpu(&st->eq_lo),
+                             eh = hi != lo ? ld_relaxed_gpu(&st->eq_hi) : 0ull,
+                             inside = ld_relaxed_gpu(&st->cand_fill);
+    const bool overflow = *(volatile uint32_t*)&st->overflow != 0;
+    int mode = 0;  // 0: restart over the input, 1: answer written, 2: continue in the candidates
+    if (k >= b && k < b + el) {
+      *out = lo;
+      mode = 1;
+    } else if (k >= b + el && k < b + el + inside) {
+      mode = overflow ? 0 : 2;
+    } else if (k >= b + el + inside && k < b + el + inside + eh) {
+      *out = hi;
+      mode = 1;
+    }
+    if (mode == 1) st->done = 1;
+    if (mode == 2) {  // the first step counts the candidates' top digit
+      st->k = k - b - el;
+      st->count = inside;
+      st->cand_n[0] = inside;
+      st->src = 1;
+    }
+    if (mode == 0) {  // an unrepresentative sample: the plain narrowing over the input
+      st->count = n;
+      st->src = 0;
+      st->overflow = 0;
+    }
+    st->cand_fill = 0;
+    st->ticket = 0;
+  }
+}
+
+// One narrowing step on digit `shift`: counts the digit over the current
+// source's keys sharing the prefix, optionally copies them to the next
+// candidate buffer; the last CTA picks.  Returns at once unless this digit
+// is the next undecided one.
+template <typename K>
+__global__ void __launch_bounds__(kSelBlock, 1) select_step_kernel(const K* keys, size_t n, K* cand_a, size_t cap_a,
+                                                                   K* cand_b, size_t cap_b, SelectState* st,
+                                                                   uint32_t shift, K* out) {
+  extern __shared__ __align__(128) unsigned char seg_smem[];
+  constexpr uint32_t W = 8u * sizeof(K);
+  // The state read here changes only in the last CTA, after every CTA has
+  // taken its ticket (or in an earlier launch).
+  if (st->done || st->prefix_bits != W - 8u - shift) return;
+  __shared__ uint32_t s_h[256 * kSelLanes];
+  __shared__ bool s_last;
+  for (uint32_t i = threadIdx.x; i < 256u * kSelLanes; i += kSelBlock) s_h[i] = 0;
+  const unsigned long long prefix = st->prefix;
+  const uint32_t prefix_bits = st->prefix_bits;
+  const uint32_t src = st->src;
+  const K* in = src == 0 ? keys : src == 1 ? cand_a : cand_b;
+  const size_t len = src == 0 ? n : (size_t)st->cand_n[src - 1];
+  K* dst = src == 0 ? cand_a : cand_b;
+  const size_t cap = src == 0 ? cap_a : cap_b;
+  // compaction goes one buffer further each time, so it never overlaps its
+  // own source
+  const bool compact = src < 2 && st->count <= (unsigned long long)cap;
+  __syncthreads();
+  const uint32_t warp = threadIdx.x >> 5;
+  K* seg = reinterpret_cast<K*>(seg_smem) + (size_t)warp * kSegKeys<K>;
+  uint32_t fill = 0;
+  uint32_t* my = s_h + (threadIdx.x % kSelLanes);
+  bool counted = false;
+  stream_keys<K>(in, len, [&](const K* kk, uint32_t valid, int nk) {
+    uint32_t mm = 0;
+    for (int e = 0; e < nk; ++e) {
+      if (((valid >> e) & 1u) && matches(kk[e], prefix, prefix_bits)) {
+        atomicAdd(my + (((uint32_t)(kk[e] >> shift) & 255u) * kSelLanes), 1u);
+        counted = true;
+        mm |= 1u << e;
+      }
+    }
+    if (compact) seg_append<K>(kk, mm, nk, seg, fill, dst, cap, st);
+  });
+  if (compact) seg_flush<K>(seg, fill, dst, cap, st);
+  fold_counts(s_h, st, counted);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  pick_bin<K>(st, st->hist, compact, out);
 }
 
 template <typename K>
 cudaError_t launch_select_t(const K* keys, size_t n, K* cand, size_t cand_cap, SelectState* st, K* out,
                             uint32_t* err, cudaStream_t stream) {
   constexpr uint32_t W = 8u * sizeof(K);
-  // step 0: the one-read histogram kernel counts every digit of 32-bit keys
-  // (the lower digits serve steps whose prefix all keys share, such as a
-  // constant input); for 64-bit keys eight digits cost more than the reads
-  // they save, so it counts only the top digit
-  cudaError_t e = sizeof(K) == 4
-                      ? launch_digit_counts(keys, n, 4, 4, 8, 0, 8, false, &st->hist_all[0][0], stream)
-                      : launch_digit_counts(keys, n, 8, 1, 8, W - 8, 0, false, &st->hist_all[W / 8 - 1][0], stream);
+  (void)err;  // no kernel of the select waits on another CTA's progress
+  // buffer A takes the range pass's candidates (or the first compaction of
+  // the input), buffer B the compaction after the next digit; A's length is
+  // a whole number of 16-byte vectors so that B stays aligned
+  size_t cap_b = cand_cap / 8;
+  size_t cap_a = (cand_cap - cap_b) & ~(size_t)(16 / sizeof(K) - 1);
+  cap_b = cand_cap - cap_a;
+  K* cand_a = cand;
+  K* cand_b = cand + cap_a;
+  const size_t sample_smem = (size_t)kSample * sizeof(K);
+  cudaError_t e = ensure_dynamic_smem(select_sample_kernel<K>, sample_smem);
   if (e != cudaSuccess) return e;
-  select_pick_kernel<K><<<1, 256, 0, stream>>>(st, out);
+  select_sample_kernel<K><<<1, kSampleThreads, sample_smem, stream>>>(keys, n, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  e = ensure_dynamic_smem(select_step_kernel<K>, Ring::kBytes);
+  const unsigned grid = (unsigned)max(1, device_info().sm_count);  // one CTA per SM
+  e = ensure_dynamic_smem(select_range_kernel<K>, kStreamSmem);
   if (e != cudaSuccess) return e;
-  const unsigned grid = (unsigned)max(1, device_info().sm_count * 2);  // two CTAs per SM
-  for (uint32_t s = 1; s < W / 8; ++s) {
+  select_range_kernel<K><<<grid, kSelBlock, kStreamSmem, stream>>>(keys, n, cand_a, cap_a, st, out);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = ensure_dynamic_smem(select_step_kernel<K>, kStreamSmem);
+  if (e != cudaSuccess) return e;
+  for (uint32_t s = 0; s < W / 8; ++s) {
     const uint32_t shift = W - 8u * (s + 1);
-    select_step_kernel<K><<<grid, kSelBlock, Ring::kBytes, stream>>>(keys, n, cand, cand_cap, st, shift, out, err);
+    select_step_kernel<K><<<grid, kSelBlock, kStreamSmem, stream>>>(keys, n, cand_a, cap_a, cand_b, cap_b, st,
+                                                                        shift, out);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
-__global__ void select_init_kernel(SelectState* st, unsigned long long k, unsigned long long n, uint32_t all_digits) {
+__global__ void select_init_kernel(SelectState* st, unsigned long long k) {
   for (int i = threadIdx.x; i < 256; i += blockDim.x) st->hist[i] = 0;
-  for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&st->hist_all[0][0])[i] = 0;
   if (threadIdx.x == 0) {
     st->prefix = 0;
     st->k = k;
-    st->count = n;
-    st->cand_n = 0;
+    st->count = 0;
+    st->cand_n[0] = st->cand_n[1] = 0;
     st->cand_fill = 0;
+    st->lo = st->hi = 0;
+    st->below = st->eq_lo = st->eq_hi = 0;
     st->prefix_bits = 0;
     st->src = 0;
     st->ticket = 0;
-    st->all_digits = all_digits;
+    st->done = 0;
+    st->overflow = 0;
   }
 }
 
@@ -297,7 +530,7 @@ size_t select_state_bytes() { return sizeof(SelectState); }
 cudaError_t launch_select(const void* keys, size_t n, size_t k, int key_bytes, void* cand, size_t cand_cap,
                           void* work, void* out, uint32_t* err, cudaStream_t stream) {
   SelectState* st = static_cast<SelectState*>(work);
-  select_init_kernel<<<1, 256, 0, stream>>>(st, k, n, key_bytes == 4 ? 1u : 0u);
+  select_init_kernel<<<1, 256, 0, stream>>>(st, k);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (key_bytes == 4)

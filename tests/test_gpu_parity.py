@@ -174,6 +174,41 @@ def test_select_matches_oracle(pa, port, n):
         assert pa.SelectRadix(a.copy(), start, length, k) == port.select(a, k, start=start, length=length)
 
 
+def test_select_sample_bracket_paths(pa, port):
+    """Select reads the input once against a bracket [lo, hi] taken from 8192
+    keys at even strides (position (j n + n / 2) / 8192).  Inputs here put
+    rank k at lo or hi, between them, outside them (the strided sample sees
+    only one value), and make the keys between them overflow the candidate
+    buffer; every case must give the oracle's answer."""
+    rng = np.random.default_rng(77)
+    n = 8192 * 4  # sampled positions are 2 (mod 4)
+    sampled = np.zeros(n, bool)
+    sampled[2::4] = True
+    # the sample sees only zeros: the bracket collapses to [0, 0] and rank n/2 lies above it
+    a = rng.integers(1 << 20, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    a[sampled] = 0
+    # the sample spreads over all 32 bits, the other keys crowd the middle: the
+    # keys strictly inside the bracket outnumber the candidate buffer
+    b = rng.integers((1 << 31) - (1 << 26) + 1, (1 << 31) + (1 << 26), n, dtype=np.uint64).astype(np.uint32)
+    b[sampled] = np.arange(8192, dtype=np.uint32) << np.uint32(19)
+    # a handful of values: rank k usually falls on lo or hi themselves
+    c = rng.integers(0, 5, n, dtype=np.uint32) * np.uint32(1000)
+    # 60 % zeros then 40 % 77s in every ten keys: rank 0.61 n is the bracket's hi
+    d = (np.arange(n) % 10 >= 6).astype(np.uint32) * np.uint32(77)
+    for name, x in (("sample_zeros", a), ("overflow", b), ("five_values", c), ("two_values", d)):
+        for k in sorted({0, 1, n // 4, n // 2, n // 2 + 1, int(n * 0.61), 3 * n // 4, n - 2, n - 1}):
+            assert pa.select(x, k) == port.select(x, k), (name, k)
+    for m in (100003, 1 << 20):  # many ranks of a uniform and a Zipf input
+        u = u32_inputs(m)["uniform"]
+        z = np.minimum(rng.zipf(1.3, m), 1 << 31).astype(np.uint32)
+        for k in rng.integers(0, m, 12):
+            assert pa.select(u, int(k)) == port.select(u, int(k)), ("uniform", m, k)
+            assert pa.select(z, int(k)) == port.select(z, int(k)), ("zipf", m, k)
+    a64 = a.astype(np.uint64) << np.uint64(31)
+    for k in (0, n // 2, n - 1):
+        assert pa.select(a64, k) == port.select(a64, k), ("sample_zeros_u64", k)
+
+
 @pytest.mark.parametrize("n", [1, 99, 100003, 1 << 20])
 def test_select_u64(pa, port, n):
     from parallelalgorithms_gb300 import workloads
