@@ -243,43 +243,59 @@ int pipelined_host_sort(Workspace* ws, cudaStream_t stream, void* keys, size_t n
   if (!ws->copy_stream) PA_CUDA(cudaStreamCreateWithFlags(&ws->copy_stream, cudaStreamNonBlocking));
   for (auto& e : ws->pipe_ev)
     if (!e) PA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  const uint32_t top_shift = 8u * (uint32_t)kb - 8u;
+  // 32-bit keys: each chunk is sorted on its top 16 bits as it arrives, and
+  // each group of top-byte buckets is finished by sorting its 16-bit buckets
+  // (gathered from every chunk) on their low 16 bits in shared memory.
+  // 64-bit keys: each chunk is split on its top byte, and each group is
+  // gathered bucket by bucket and sorted by the plain sort.
+  const bool b16 = kb == 4;
+  const int cpass = b16 ? 2 : 1;  // digit passes per chunk
+  const uint32_t shift0 = b16 ? 16u : 8u * (uint32_t)kb - 8u;
   const size_t chunk = ((n + kPipeChunks - 1) / kPipeChunks + 3) & ~(size_t)3;
+  if (b16 && chunk >= ((size_t)1 << 32))  // (bucket bounds are 32-bit chunk offsets)
+    return set_error(PA_ERR_OOM, "chunks of 2^32 keys or more take the two-buffer path");
   const size_t ctiles = ceil_div(chunk, onesweep_tile_keys(kb, false));
   const size_t sb = onesweep_status_bytes(chunk);
-  // 32-bit groups are sorted bucket by bucket by the batched kernel (three
-  // passes: a bucket's top byte is constant); its plan block is bounded by
-  // n / 2 bytes of look-back words plus tables.
-  const size_t plan_cap = kb == 4 ? n / 2 + ((size_t)8 << 20) : 0;
+  const size_t pstat = ctiles * 256 * sb;  // one chunk pass's look-back words
+  // groups that fall back to the batched kernel (a 16-bit bucket past the
+  // shared-memory sort) need its plan block: n / 2 bytes of look-back words
+  // plus tables at most
+  const size_t plan_cap = b16 ? n / 2 + ((size_t)8 << 20) : 0;
+  constexpr size_t kStarts = 65537;  // 16-bit bucket starts per chunk
   char *d_keys = nullptr, *d_tmp = nullptr, *d_gs = nullptr, *status = nullptr, *gscratch = nullptr, *plan_dev = nullptr;
-  unsigned long long *counts = nullptr, *bin_start = nullptr, *runs = nullptr;
-  uint32_t* tile_ctr = nullptr;
+  unsigned long long *counts = nullptr, *bin_start = nullptr, *runs = nullptr, *pos16 = nullptr, *summary = nullptr;
+  uint32_t *tile_ctr = nullptr, *starts = nullptr, *btot = nullptr;
   SortCtrl* ctrl = nullptr;
   constexpr size_t kMaxRuns = (size_t)256 * kPipeChunks;  // every (bucket, chunk) piece
   auto layout = [&](Carve& c) {
-    d_keys = c.take<char>(n * kb);  // input chunks; later the gathered groups
-    d_tmp = c.take<char>(n * kb);   // chunks split into buckets
-    d_gs = c.take<char>(n * kb);    // the group sorts' scratch (and 3-pass results)
-    counts = c.take<unsigned long long>((size_t)kPipeChunks * 256);
-    tile_ctr = c.take<uint32_t>(kPipeChunks);
-    status = c.take<char>((size_t)kPipeChunks * ctiles * 256 * sb);
-    bin_start = c.take<unsigned long long>((size_t)kPipeChunks * 256);
+    d_keys = c.take<char>(n * kb);  // input chunks (32-bit: then sorted on the top 16 bits)
+    d_tmp = c.take<char>(n * kb);   // 64-bit: chunks split on the top byte; 32-bit: the result
+    d_gs = c.take<char>(n * kb);    // the group sorts' scratch
+    counts = c.take<unsigned long long>((size_t)kPipeChunks * cpass * 256);
+    tile_ctr = c.take<uint32_t>((size_t)kPipeChunks * cpass);
+    status = c.take<char>((size_t)kPipeChunks * cpass * pstat);
+    bin_start = c.take<unsigned long long>((size_t)kPipeChunks * cpass * 256);
     ctrl = c.take<SortCtrl>(kPipeChunks);
     runs = c.take<unsigned long long>(kMaxRuns * 3);
     gscratch = c.take<char>(sort_scratch_bytes(n, kb, false));
     plan_dev = c.take<char>(plan_cap);
+    starts = c.take<uint32_t>(b16 ? (size_t)kPipeChunks * kStarts : 0);
+    pos16 = c.take<unsigned long long>(b16 ? kStarts : 0);
+    btot = c.take<uint32_t>(b16 ? kStarts : 0);
+    summary = c.take<unsigned long long>(b16 ? 512 : 0);
   };
   Carve m{nullptr};
   layout(m);
   if (int rc = ensure_dev(ws, stream, m.off)) return rc;
   Carve r{ws->dev};
   layout(r);
-  const size_t zero_bytes = (size_t)(status + (size_t)kPipeChunks * ctiles * 256 * sb - reinterpret_cast<char*>(counts));
+  const size_t zero_bytes = (size_t)(status + (size_t)kPipeChunks * cpass * pstat - reinterpret_cast<char*>(counts));
   cudaEvent_t* ev = ws->pipe_ev;
   cudaStream_t cs = ws->copy_stream;
   char* h = static_cast<char*>(keys);
 
-  // 1. chunked copy-in; each arrived chunk is counted and split by its top digit
+  // 1. chunked copy-in; each arrived chunk is counted and sorted on its top
+  //    16 bits (32-bit keys) or split on its top byte (64-bit keys)
   PA_CUDA(cudaMemsetAsync(counts, 0, zero_bytes, stream));
   PA_CUDA(cudaEventRecord(ev[0], stream));  // earlier work on this workspace is ordered before the copies
   PA_CUDA(cudaStreamWaitEvent(cs, ev[0], 0));
@@ -292,34 +308,47 @@ int pipelined_host_sort(Workspace* ws, cudaStream_t stream, void* keys, size_t n
     PA_CUDA(cudaMemcpyAsync(d_keys + lo * kb, h + lo * kb, (hi - lo) * kb, cudaMemcpyHostToDevice, cs));
     PA_CUDA(cudaEventRecord(ev[1 + c], cs));
     PA_CUDA(cudaStreamWaitEvent(stream, ev[1 + c], 0));
-    unsigned long long* cnt = counts + (size_t)c * 256;
-    unsigned long long* bs = bin_start + (size_t)c * 256;
-    PA_CUDA(launch_digit_counts(d_keys + lo * kb, hi - lo, kb, 1, 8, top_shift, 0, false, cnt, stream));
-    PA_CUDA(launch_scan_digits(cnt, 1, 8, hi - lo, false, false, bs, &ctrl[c], stream));
-    OnesweepArgs a{};
-    a.keys_a = d_keys + lo * kb;
-    a.keys_b = d_tmp + lo * kb;
-    a.n = hi - lo;
-    a.shift = top_shift;
-    a.pass = 0;
-    a.bin_start = bs;
-    a.status = status + (size_t)c * ctiles * 256 * sb;
-    a.tile_counter = tile_ctr + c;
-    a.ctrl = &ctrl[c];
-    a.err = ws->err;
-    PA_CUDA(launch_onesweep_pass(a, kb, false, stream));
+    unsigned long long* cnt = counts + (size_t)c * cpass * 256;
+    unsigned long long* bs = bin_start + (size_t)c * cpass * 256;
+    PA_CUDA(launch_digit_counts(d_keys + lo * kb, hi - lo, kb, cpass, 8, shift0, 8, false, cnt, stream));
+    PA_CUDA(launch_scan_digits(cnt, cpass, 8, hi - lo, false, false, bs, &ctrl[c], stream));
+    for (int p = 0; p < cpass; ++p) {  // (no pass is skipped: two passes end back in d_keys)
+      OnesweepArgs a{};
+      a.keys_a = d_keys + lo * kb;
+      a.keys_b = d_tmp + lo * kb;
+      a.n = hi - lo;
+      a.shift = shift0 + 8u * (uint32_t)p;
+      a.pass = p;
+      a.bin_start = bs + (size_t)p * 256;
+      a.status = status + ((size_t)c * cpass + p) * pstat;
+      a.tile_counter = tile_ctr + (size_t)c * cpass + p;
+      a.ctrl = &ctrl[c];
+      a.err = ws->err;
+      PA_CUDA(launch_onesweep_pass(a, kb, false, stream));
+    }
+    if (b16)
+      PA_CUDA(launch_bucket_bounds(reinterpret_cast<const uint32_t*>(d_keys) + lo, hi - lo, bs + 256,
+                                   starts + (size_t)c * kStarts, stream));
   }
   clo[nc] = n;
-  std::vector<unsigned long long> hc((size_t)nc * 256);  // [chunks][256] counts
+  char* split = b16 ? d_keys : d_tmp;  // where each chunk's top-byte buckets lie, in order
+  if (b16) PA_CUDA(launch_bucket_totals(starts, nc, btot, pos16, summary, stream));
+  std::vector<unsigned long long> hc((size_t)nc * 256);  // [chunks][256] top-byte counts
+  std::vector<unsigned long long> bmax(256, 0);           // largest 16-bit bucket per top byte
   {
-    unsigned long long* stage = static_cast<unsigned long long*>(pipe_pinned(ws, (size_t)nc * 256 * 8));
+    const size_t cbytes = (size_t)nc * cpass * 256 * 8;
+    unsigned long long* stage =
+        static_cast<unsigned long long*>(pipe_pinned(ws, cbytes + (b16 ? 512 * 8 : 0)));
     if (!stage) return set_error(PA_ERR_OOM, "page-locked staging for the pipelined sort");
-    PA_CUDA(cudaMemcpyAsync(stage, counts, (size_t)nc * 256 * 8, cudaMemcpyDeviceToHost, stream));
+    PA_CUDA(cudaMemcpyAsync(stage, counts, cbytes, cudaMemcpyDeviceToHost, stream));
+    if (b16) PA_CUDA(cudaMemcpyAsync(stage + cbytes / 8, summary, 512 * 8, cudaMemcpyDeviceToHost, stream));
     PA_CUDA(cudaStreamSynchronize(stream));
-    std::memcpy(hc.data(), stage, hc.size() * 8);
+    for (int c = 0; c < nc; ++c)
+      std::memcpy(&hc[(size_t)c * 256], stage + ((size_t)c * cpass + cpass - 1) * 256, 256 * 8);
+    if (b16) std::memcpy(bmax.data(), stage + cbytes / 8 + 256, 256 * 8);
   }
 
-  // 2. groups of whole buckets; each group's runs, bucket by bucket, one per chunk
+  // 2. groups of whole top-byte buckets
   unsigned long long total[257] = {};
   for (int b = 0; b < 256; ++b)
     for (int c = 0; c < nc; ++c) total[b + 1] += hc[(size_t)c * 256 + b];
@@ -333,16 +362,25 @@ int pipelined_host_sort(Workspace* ws, cudaStream_t stream, void* keys, size_t n
   for (int b = 1; b < 256 && ng < want_groups - 1; ++b)
     if (total[b] - total[gb[ng]] >= share && total[b] < n) gb[++ng] = b;
   gb[++ng] = 256;
-  // bucket b of chunk c starts at clo[c] + (its counts of buckets < b) in d_tmp
+  // 32-bit groups whose 16-bit buckets all fit the shared-memory sort take
+  // it; the others (and every 64-bit group) are gathered bucket by bucket
+  std::vector<size_t> gmax(ng, 0);
+  std::vector<bool> fast(ng, false);
+  for (int g = 0; g < ng; ++g) {
+    for (int b = gb[g]; b < gb[g + 1]; ++b) gmax[g] = std::max<size_t>(gmax[g], (size_t)bmax[b]);
+    fast[g] = b16 && gmax[g] <= bucket_sort_max_keys();
+  }
+  // bucket b of chunk c starts at clo[c] + (its counts of buckets < b) in `split`
   std::vector<unsigned long long> local((size_t)nc * 257);
   for (int c = 0; c < nc; ++c) {
     local[(size_t)c * 257] = 0;
     for (int b = 0; b < 256; ++b) local[(size_t)c * 257 + b + 1] = local[(size_t)c * 257 + b] + hc[(size_t)c * 256 + b];
   }
-  std::vector<unsigned long long> run_tab;  // (src, len, dst) triples, group by group
+  std::vector<unsigned long long> run_tab;  // (src, len, dst) triples of the gathered groups
   std::vector<size_t> run_first(ng + 1), run_max(ng, 0);
   for (int g = 0; g < ng; ++g) {
     run_first[g] = run_tab.size() / 3;
+    if (fast[g]) continue;
     const unsigned long long g0 = total[gb[g]];
     for (int b = gb[g]; b < gb[g + 1]; ++b)
       for (int c = 0; c < nc; ++c) {
@@ -355,48 +393,67 @@ int pipelined_host_sort(Workspace* ws, cudaStream_t stream, void* keys, size_t n
       }
   }
   run_first[ng] = run_tab.size() / 3;
-  // per-group batched plans (32-bit keys): buckets as segments, three passes
-  std::vector<seg::HostPlan> plans(kb == 4 ? ng : 0);
+  // gathered 32-bit groups: batched plans with the buckets as segments and
+  // three passes (a bucket's top byte is constant); a plan past the batched
+  // sort's limits leaves its group to the plain sort
+  std::vector<seg::HostPlan> plans(b16 ? ng : 0);
+  std::vector<bool> planned(ng, false);
   std::vector<size_t> image_off(ng + 1, 0);
-  bool batched = kb == 4;
-  for (int g = 0; g < ng && batched; ++g) {
-    std::vector<uint64_t> off(gb[g + 1] - gb[g] + 1);
-    for (int b = gb[g]; b <= gb[g + 1]; ++b) off[b - gb[g]] = total[b] - total[gb[g]];
-    pa_segsort_config cfg{};
-    cfg.small_cutoff = 4096;
-    cfg.tile_keys = 8192;
-    if (seg::build_host_plan(off.data(), off.size() - 1, &cfg, &plans[g], 3) != PA_OK || plans[g].bytes > plan_cap)
-      batched = false;  // (a bucket past the batched sort's limits) the plain sort takes the groups
-    image_off[g + 1] = image_off[g] + ((batched ? seg::plan_image_bytes(plans[g]) : 0) + 255) / 256 * 256;
+  for (int g = 0; g < ng; ++g) {
+    size_t bytes = 0;
+    if (b16 && !fast[g]) {
+      std::vector<uint64_t> off(gb[g + 1] - gb[g] + 1);
+      for (int b = gb[g]; b <= gb[g + 1]; ++b) off[b - gb[g]] = total[b] - total[gb[g]];
+      pa_segsort_config cfg{};
+      cfg.small_cutoff = 4096;
+      cfg.tile_keys = 8192;
+      planned[g] = seg::build_host_plan(off.data(), off.size() - 1, &cfg, &plans[g], 3) == PA_OK &&
+                   plans[g].bytes <= plan_cap;
+      if (planned[g]) bytes = seg::plan_image_bytes(plans[g]);
+    }
+    image_off[g + 1] = image_off[g] + (bytes + 255) / 256 * 256;
   }
-  if (!batched) std::fill(image_off.begin(), image_off.end(), 0);
   const size_t runs_bytes = run_tab.size() * 8;
   const size_t images_at = (runs_bytes + 255) / 256 * 256;  // the plan images follow the run table
-  char* stage = static_cast<char*>(pipe_pinned(ws, images_at + image_off[ng]));
+  char* stage = static_cast<char*>(pipe_pinned(ws, images_at + image_off[ng] + 256));
   if (!stage) return set_error(PA_ERR_OOM, "page-locked staging for the pipelined sort");
-  std::memcpy(stage, run_tab.data(), runs_bytes);
-  PA_CUDA(cudaMemcpyAsync(runs, stage, runs_bytes, cudaMemcpyHostToDevice, stream));
+  if (runs_bytes) {
+    std::memcpy(stage, run_tab.data(), runs_bytes);
+    PA_CUDA(cudaMemcpyAsync(runs, stage, runs_bytes, cudaMemcpyHostToDevice, stream));
+  }
   char* images = stage + images_at;
+  ChunkRuns chunks{};
+  chunks.count = nc;
+  for (int c = 0; c < nc; ++c) chunks.lo[c] = clo[c];
 
-  // 3. per group: gather, sort, copy out while the next group runs
+  // 3. per group: sort, copy out while the next group runs
   for (int g = 0; g < ng; ++g) {
     const size_t lo = (size_t)total[gb[g]], len = (size_t)(total[gb[g + 1]] - total[gb[g]]);
     if (len == 0) continue;
-    PA_CUDA(launch_gather_runs(d_tmp, d_keys + lo * kb, runs + run_first[g] * 3, run_first[g + 1] - run_first[g],
-                               run_max[g], kb, stream));
-    char* result = d_keys + lo * kb;
-    if (batched) {
-      seg::HostPlan& hp = plans[g];
-      PA_CUDA(seg::upload_plan(hp, plan_dev, stream, images + image_off[g]));
-      seg::PlanDev pd = seg::device_view(hp, plan_dev, reinterpret_cast<uint32_t*>(d_keys + lo * kb),
-                                         reinterpret_cast<uint32_t*>(d_gs + lo * kb));
-      pd.err = ws->err;
-      PA_CUDA(seg::launch_plan(hp, pd, plan_dev, seg::plan_grid(hp), stream));
-      result = reinterpret_cast<char*>(seg::result_buffer(pd));
+    char* result = nullptr;
+    if (fast[g]) {
+      PA_CUDA(launch_bucket_sort(reinterpret_cast<const uint32_t*>(d_keys), chunks, starts, pos16,
+                                 (uint32_t)gb[g] * 256u, (uint32_t)(gb[g + 1] - gb[g]) * 256u, gmax[g],
+                                 reinterpret_cast<uint32_t*>(d_tmp), ws->err, stream));
+      result = d_tmp + lo * kb;
     } else {
-      SortScratch sc{};
-      sort_scratch_layout(gscratch, len, kb, false, &sc);
-      PA_CUDA(enqueue_sort(sc, d_keys + lo * kb, d_gs + lo * kb, nullptr, nullptr, len, kb, false, ws->err, stream));
+      char* gdst = b16 ? d_tmp : d_keys;  // the buffer the chunks' buckets are not in
+      PA_CUDA(launch_gather_runs(split, gdst + lo * kb, runs + run_first[g] * 3, run_first[g + 1] - run_first[g],
+                                 run_max[g], kb, stream));
+      result = gdst + lo * kb;
+      if (planned[g]) {
+        seg::HostPlan& hp = plans[g];
+        PA_CUDA(seg::upload_plan(hp, plan_dev, stream, images + image_off[g]));
+        seg::PlanDev pd = seg::device_view(hp, plan_dev, reinterpret_cast<uint32_t*>(gdst + lo * kb),
+                                           reinterpret_cast<uint32_t*>(d_gs + lo * kb));
+        pd.err = ws->err;
+        PA_CUDA(seg::launch_plan(hp, pd, plan_dev, seg::plan_grid(hp), stream));
+        result = reinterpret_cast<char*>(seg::result_buffer(pd));
+      } else {
+        SortScratch sc{};
+        sort_scratch_layout(gscratch, len, kb, false, &sc);
+        PA_CUDA(enqueue_sort(sc, gdst + lo * kb, d_gs + lo * kb, nullptr, nullptr, len, kb, false, ws->err, stream));
+      }
     }
     PA_CUDA(cudaEventRecord(ev[1 + kPipeChunks + g], stream));
     PA_CUDA(cudaStreamWaitEvent(cs, ev[1 + kPipeChunks + g], 0));

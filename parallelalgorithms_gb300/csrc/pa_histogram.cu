@@ -251,6 +251,7 @@ cudaError_t launch_digit_counts(const void* keys, size_t n, int key_bytes, int n
   if (radix_bits == 8) {
     if (key_bytes == 4) {
       if (num_digits == 4) return launch_counts_t<uint32_t, 4, 8>(keys, n, shift0, shift_step, is_float, out, stream);
+      if (num_digits == 2) return launch_counts_t<uint32_t, 2, 8>(keys, n, shift0, shift_step, is_float, out, stream);
       if (num_digits == 1) return launch_counts_t<uint32_t, 1, 8>(keys, n, shift0, shift_step, is_float, out, stream);
     } else if (key_bytes == 8) {
       if (num_digits == 8)

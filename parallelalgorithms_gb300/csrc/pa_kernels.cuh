@@ -116,6 +116,31 @@ cudaError_t launch_small_sort(void* keys, uint32_t* vals, size_t n, int key_byte
 cudaError_t launch_gather_runs(const void* src, void* dst, const unsigned long long* runs, size_t nruns,
                                size_t max_run, int key_bytes, cudaStream_t stream);
 
+// ---- pipelined host-buffer sort of 32-bit keys (pa_pipeline.cu) -----------
+// Chunks sorted on their top 16 bits, then 16-bit buckets gathered from
+// every chunk and sorted on their low 16 bits into their final places.
+constexpr int kMaxChunkRuns = 8;
+struct ChunkRuns {
+  unsigned long long lo[kMaxChunkRuns];  // first key of each chunk in the source buffer
+  int count;
+};
+// starts[0, 65536]: where each 16-bit bucket starts in keys[0, n) (sorted on
+// the top 16 bits; n < 2^32); top_start: the 256 exclusive top-byte starts.
+cudaError_t launch_bucket_bounds(const uint32_t* keys, size_t n, const unsigned long long* top_start, uint32_t* starts,
+                                 cudaStream_t stream);
+// From the chunks' starts ([num_chunks][65537]): tot[0, 65536) each
+// bucket's keys, pos[0, 65536] the buckets' global starts; summary[0, 256)
+// keys per top byte, summary[256, 512) the largest 16-bit bucket of each.
+cudaError_t launch_bucket_totals(const uint32_t* starts, int num_chunks, uint32_t* tot, unsigned long long* pos,
+                                 unsigned long long* summary, cudaStream_t stream);
+// Buckets [first_bucket, + num_buckets), none larger than max_bucket_keys
+// (at most bucket_sort_max_keys()): gathered from src, sorted, written to
+// dst[pos[b], pos[b + 1]).
+size_t bucket_sort_max_keys();
+cudaError_t launch_bucket_sort(const uint32_t* src, const ChunkRuns& chunks, const uint32_t* starts,
+                               const unsigned long long* pos, uint32_t first_bucket, uint32_t num_buckets,
+                               size_t max_bucket_keys, uint32_t* dst, uint32_t* err, cudaStream_t stream);
+
 // Copies the result back into the caller's buffers when the executed passes
 // left it in the scratch buffers (device-side decision from SortCtrl).
 cudaError_t launch_final_copy(void* keys_a, const void* keys_b, uint32_t* vals_a, const uint32_t* vals_b,

@@ -1,9 +1,10 @@
 """Host-buffer sorts of 2^24 keys or more take the pipelined path (chunked
-copy-in with top-digit counts, one top-digit pass, bucket groups sorted and
+copy-in; each chunk sorted on its top 16 bits (32-bit keys) or split on its
+top byte (64-bit keys) as it arrives; groups of top-byte buckets finished and
 copied out in turn).  Its result must equal the oracle's bit for bit, for
-inputs that exercise the grouping: uniform, presorted, constant (one bucket
-holds every key: the top-digit pass is skipped), two buckets only, a
-heavy bucket beside light ones, and 64-bit keys."""
+inputs that exercise the grouping and both ways a 32-bit group is finished:
+uniform, presorted, constant, two buckets only, a heavy bucket beside light
+ones, buckets at the shared-memory sort's size limits, and 64-bit keys."""
 import numpy as np
 import pytest
 
@@ -33,6 +34,31 @@ def test_pipelined_host_sort_u32(pa, port, name):
     got2, tmp = a.copy(), np.zeros_like(a)
     pa.SortRadixPar(got2, tmp, a.size)
     np.testing.assert_array_equal(got2, want)
+
+
+def test_pipelined_bucket_sizes_at_the_shared_memory_limits(pa, port):
+    """32-bit groups whose 16-bit buckets (keys sharing their top 16 bits)
+    all hold at most 8192 keys are sorted bucket by bucket in shared memory,
+    by a 2048-, 4096- or 8192-key tile picked from the group's largest
+    bucket; a group with a larger bucket falls back to the batched sort.
+    Buckets of exactly 2048, 2049, 4096, 4097, 8192 and 8193 keys, each in a
+    top byte of its own, exercise every boundary."""
+    from parallelalgorithms_gb300 import workloads
+    u = workloads.uniform_u32(N)
+    rng = np.random.default_rng(3)
+    donors = np.flatnonzero((u >> np.uint32(24)) >= 0x80)  # keys moved into the buckets below
+    used = 0
+    for top16, size in ((0x1100, 2048), (0x2200, 2049), (0x3300, 4096), (0x4400, 4097), (0x5500, 8192),
+                        (0x6600, 8193)):
+        need = size - int(np.count_nonzero((u >> np.uint32(16)) == top16))
+        pick = donors[used:used + need]
+        used += need
+        u[pick] = (np.uint32(top16) << np.uint32(16)) | rng.integers(0, 1 << 16, need, dtype=np.uint32)
+        assert int(np.count_nonzero((u >> np.uint32(16)) == top16)) == size
+    want, _ = port.sort(u)
+    got = u.copy()
+    pa.sort(got)
+    np.testing.assert_array_equal(got, want)
 
 
 def test_pipelined_host_sort_u64(pa, port):
