@@ -6,8 +6,9 @@
 // keys together (MoveOutsideOfKthBinIn, :36-55), recurse into the bin.  The
 // result is the same order statistic; here the input is read once in the
 // usual case and never moved:
-//   sample   one CTA takes kSample keys at even strides and finds, by the
-//            same MSD digit narrowing in shared memory, the sample's keys
+//   sample   eight CTAs take kSample keys at even strides and the last of
+//            them finds, by the same MSD digit narrowing in shared memory,
+//            the sample's keys
 //            `lo` and `hi` a few standard deviations below and above rank k
 //            (the extreme ranks give the key type's minimum / maximum);
 //   range    one streaming read of the input counts the keys below lo and
@@ -34,7 +35,10 @@
 
 namespace pa {
 
+constexpr int kSelectSample = 8192;  // keys in the bracketing sample
+
 struct SelectState {
+  unsigned long long sample[kSelectSample];  // the sample, gathered by several CTAs
   unsigned long long hist[256];
   unsigned long long prefix;        // decided high digits, right-aligned
   unsigned long long k;             // rank sought among the current source's keys sharing prefix
@@ -71,6 +75,7 @@ constexpr size_t kStreamSmem = (size_t)kSelWarps * kSegBytes;
 // for the median and the sample misses rank k with probability ~1e-6.
 constexpr int kSampleLog2 = 13;
 constexpr int kSample = 1 << kSampleLog2;
+static_assert(kSample == kSelectSample, "the state block holds the sample");
 constexpr int kSampleThreads = 1024;
 constexpr double kBracketSigmas = 5.0;
 
@@ -134,7 +139,9 @@ __device__ void pick_bin(SelectState* st, const unsigned long long* h, bool comp
 // The bracket: kSample keys at even strides, and their order statistics at
 // the ranks kBracketSigmas standard deviations either side of rank k's
 // image, both found at once by MSD digit narrowing over the sample in
-// shared memory.
+// shared memory.  kSample / kSampleThreads CTAs gather the sample (strided
+// loads over the whole input go faster from several SMs) into the state
+// block; the last of them (ticket) reads it back from L2 and narrows.
 template <typename K>
 __global__ void __launch_bounds__(kSampleThreads) select_sample_kernel(const K* keys, size_t n, SelectState* st) {
   constexpr uint32_t W = 8u * sizeof(K);
@@ -142,17 +149,30 @@ __global__ void __launch_bounds__(kSampleThreads) select_sample_kernel(const K* 
   K* s = reinterpret_cast<K*>(sample_raw);
   __shared__ uint32_t s_h[2][256];
   __shared__ unsigned long long s_pref[2], s_rank[2];
-  __shared__ bool s_lo_min, s_hi_max;
+  __shared__ bool s_lo_min, s_hi_max, s_last;
   const uint32_t tid = threadIdx.x;
   const uint32_t ns = (uint32_t)(n < (size_t)kSample ? n : (size_t)kSample);
   // key j of the sample sits at (j n + n / 2) / ns: a shift when ns is the
   // full sample (a power of two), j itself when the input is smaller
+  {
+    const uint32_t j = blockIdx.x * kSampleThreads + tid;
+    if (j < ns)
+      st->sample[j] = (unsigned long long)keys[ns == (uint32_t)kSample ? ((size_t)j * n + n / 2) >> kSampleLog2
+                                                                        : (size_t)j];
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
 #pragma unroll
-  for (int q = 0; q < kSample / kSampleThreads; ++q) {  // independent loads, all in flight at once
+  for (int q = 0; q < kSample / kSampleThreads; ++q) {  // (L2 reads: other SMs wrote them)
     const uint32_t j = tid + (uint32_t)q * kSampleThreads;
-    if (j < ns) s[j] = keys[ns == (uint32_t)kSample ? ((size_t)j * n + n / 2) >> kSampleLog2 : (size_t)j];
+    if (j < ns) s[j] = (K)__ldcg(&st->sample[j]);
   }
   if (tid == 0) {
+    st->ticket = 0;
     const double p = ((double)st->k + 0.5) / (double)n;
     long long r = (long long)(p * (double)ns);
     if (r > (long long)ns - 1) r = (long long)ns - 1;
@@ -484,7 +504,7 @@ cudaError_t launch_select_t(const K* keys, size_t n, K* cand, size_t cand_cap, S
   const size_t sample_smem = (size_t)kSample * sizeof(K);
   cudaError_t e = ensure_dynamic_smem(select_sample_kernel<K>, sample_smem);
   if (e != cudaSuccess) return e;
-  select_sample_kernel<K><<<1, kSampleThreads, sample_smem, stream>>>(keys, n, st);
+  select_sample_kernel<K><<<kSample / kSampleThreads, kSampleThreads, sample_smem, stream>>>(keys, n, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const unsigned grid = (unsigned)max(1, device_info().sm_count);  // one CTA per SM
