@@ -6,7 +6,10 @@ Generates the seeded input once, keeps it device-resident, and runs the
 operation `reps` times with nothing else on the GPU, so that an ncu launch
 filter (-k regex:onesweep -s <skip> -c <count>) lands on known launches.
 Per sort: one digit histogram, one scan, one onesweep launch per key byte,
-one final copy (plus the workspace memset).
+one final copy (plus the workspace memset).  `sort_u32_host` sorts a
+page-locked host copy of the keys through the C ABI instead (the pipelined
+host-buffer path: chunk passes, bucket bounds and totals, group sorts, with
+the copies between them).
 """
 from __future__ import annotations
 
@@ -19,7 +22,8 @@ import numpy as np
 def main() -> None:
     p = argparse.ArgumentParser()
     p.add_argument("--op", default="sort_u32",
-                   choices=["sort_u32", "sort_u64", "sort_kv_u64", "sort_f32", "hist_u32", "select_u32", "sum_u32"])
+                   choices=["sort_u32", "sort_u32_host", "sort_u64", "sort_kv_u64", "sort_f32", "hist_u32", "select_u32",
+                            "sum_u32"])
     p.add_argument("--n", type=int, default=50_000_000)
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--dist", default="uniform", choices=["uniform", "presorted", "constant"])
@@ -52,9 +56,16 @@ def main() -> None:
     out = torch.zeros(256, dtype=torch.int64, device="cuda")
     stream = torch.cuda.current_stream()
     o = _native.opts(stream.cuda_stream)
+    host_t = host = None
+    if a.op == "sort_u32_host":
+        host_t = torch.empty(n, dtype=torch.int32, pin_memory=True)  # (kept alive for the view below)
+        host = host_t.numpy().view(np.uint32)
     for _ in range(a.reps):
         k.copy_(src)
-        if a.op == "sort_u32":
+        if a.op == "sort_u32_host":
+            np.copyto(host, keys)
+            _native.call("pa_sort_u32", P(host.ctypes.data), None, n, None)
+        elif a.op == "sort_u32":
             _native.call("pa_sort_u32", P(k.data_ptr()), P(t.data_ptr()), n, o)
         elif a.op == "sort_f32":
             _native.call("pa_sort_f32", P(k.data_ptr()), P(t.data_ptr()), n, o)
