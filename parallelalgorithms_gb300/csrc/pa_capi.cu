@@ -199,6 +199,9 @@ constexpr size_t kPipeMinKeys = (size_t)1 << 24;
 // in shared memory 0.18 ms, copying them out 0.26 ms).
 constexpr int kPipeRamp[kPipeGroups] = {1, 3, 6, 10, 16, 24, 34, 44, 54, 64};
 
+// PA_HOST_PIPELINE=0 turns the pipelined host-buffer sort off: host buffers
+// of any size then take the two-buffer path (copy in, sort, copy out), as a
+// comparison point.
 bool pipeline_enabled() {
   static const bool v = [] {
     const char* e = std::getenv("PA_HOST_PIPELINE");
