@@ -73,6 +73,7 @@ int cuda_fail(cudaError_t e, const char* what) {
 constexpr int kMaxEvents = 16;
 
 constexpr int kPipeChunks = 8;   // host-buffer sort: copy-in chunks
+static_assert(kPipeChunks <= kMaxChunkRuns, "the bucket sort's chunk table holds every chunk");
 constexpr int kPipeGroups = 10;  // host-buffer sort: bucket groups sorted and copied out in turn
 
 struct Workspace {
