@@ -15,8 +15,9 @@
 //            equal to lo and to hi and copies the keys strictly between
 //            them (the candidates) to a buffer, branch-free per key; the
 //            last CTA (ticket) then either has the answer (lo or hi), or
-//            continues with rank k among the candidates (the first step
-//            counts their top digit), or (rank k outside the bracket, or the
+//            continues with rank k among the candidates and picks their top
+//            digit (counted as each warp flushed its candidates), or (rank
+//            k outside the bracket, or the
 //            candidates overflowed: an unrepresentative sample) restarts the
 //            plain digit-by-digit narrowing over the whole input;
 //   step s   the digit below the decided prefix is counted over the keys of
@@ -238,12 +239,17 @@ __global__ void __launch_bounds__(kSampleThreads) select_sample_kernel(const K* 
 
 // A consumer warp's candidate segment in shared memory: `fill` keys (the
 // same value in every lane).  seg_flush writes them to dst with one global
-// reservation (one past the capacity only raises st->overflow);
+// reservation (one past the capacity only raises st->overflow), and with
+// `top` set also counts each written key's top digit into the lane-banked
+// shared counters at `top` (a warp-uniform loop: counting here costs far
+// less than a per-key branch while streaming);
 // seg_append adds this thread's matched keys (kk[e] where bit e of mm is
 // set), flushing first when they would not fit.  Both are warp-collective.
 template <typename K>
-__device__ __forceinline__ void seg_flush(K* seg, uint32_t& fill, K* dst, size_t cap, SelectState* st) {
+__device__ __forceinline__ void seg_flush(K* seg, uint32_t& fill, K* dst, size_t cap, SelectState* st,
+                                          uint32_t* top = nullptr) {
   constexpr uint32_t FULL = 0xFFFFFFFFu;
+  constexpr uint32_t W = 8u * sizeof(K);
   if (fill == 0) return;
   const uint32_t lane = threadIdx.x & 31u;
   unsigned long long base = 0;
@@ -251,7 +257,11 @@ __device__ __forceinline__ void seg_flush(K* seg, uint32_t& fill, K* dst, size_t
   base = __shfl_sync(FULL, base, 0);
   __syncwarp();  // every lane's segment writes are visible
   if (base + fill <= cap) {
-    for (uint32_t i = lane; i < fill; i += 32) dst[base + i] = seg[i];
+    for (uint32_t i = lane; i < fill; i += 32) {
+      const K key = seg[i];
+      dst[base + i] = key;
+      if (top) atomicAdd(top + (((uint32_t)(key >> (W - 8)) & 255u) * kSelLanes), 1u);
+    }
   } else if (lane == 0) {
     st->overflow = 1;
   }
@@ -261,7 +271,7 @@ __device__ __forceinline__ void seg_flush(K* seg, uint32_t& fill, K* dst, size_t
 
 template <typename K>
 __device__ __forceinline__ void seg_append(const K* kk, uint32_t mm, int nk, K* seg, uint32_t& fill, K* dst,
-                                           size_t cap, SelectState* st) {
+                                           size_t cap, SelectState* st, uint32_t* top = nullptr) {
   constexpr uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t cnt = __popc(mm);
@@ -273,7 +283,7 @@ __device__ __forceinline__ void seg_append(const K* kk, uint32_t mm, int nk, K* 
     if (lane >= (uint32_t)o) incl += v;
   }
   const uint32_t total = __shfl_sync(FULL, incl, 31);
-  if (fill + total > kSegKeys<K>) seg_flush<K>(seg, fill, dst, cap, st);
+  if (fill + total > kSegKeys<K>) seg_flush<K>(seg, fill, dst, cap, st, top);
   uint32_t at = fill + incl - cnt;
   for (int e = 0; e < nk; ++e)
     if ((mm >> e) & 1u) seg[at++] = kk[e];
@@ -359,8 +369,11 @@ template <typename K>
 __global__ void __launch_bounds__(kSelBlock, 1) select_range_kernel(const K* keys, size_t n, K* cand_a, size_t cap_a,
                                                                     SelectState* st, K* out) {
   extern __shared__ __align__(128) unsigned char seg_smem[];
+  __shared__ uint32_t s_h[256 * kSelLanes];  // the candidates' top digit, lane-banked
   __shared__ uint32_t s_cnt[3];
   __shared__ bool s_last;
+  __shared__ int s_mode;
+  for (uint32_t i = threadIdx.x; i < 256u * kSelLanes; i += kSelBlock) s_h[i] = 0;
   if (threadIdx.x == 0) s_cnt[0] = s_cnt[1] = s_cnt[2] = 0;
   const K lo = (K)st->lo, hi = (K)st->hi;
   // strictly inside (lo, hi)  <=>  key - (lo + 1) < hi - lo - 1 (unsigned);
@@ -370,9 +383,11 @@ __global__ void __launch_bounds__(kSelBlock, 1) select_range_kernel(const K* key
   const uint32_t warp = threadIdx.x >> 5;
   K* seg = reinterpret_cast<K*>(seg_smem) + (size_t)warp * kSegKeys<K>;
   uint32_t fill = 0;
+  uint32_t* my_top = s_h + (threadIdx.x % kSelLanes);
   uint32_t below = 0, eq_lo = 0, eq_hi = 0;
   // branch-free per key: three counts and a match bit (per-key branches
-  // or shared atomics here would cost more than the read itself)
+  // or shared atomics here would cost more than the read itself; the
+  // candidates' top digit is counted as each warp flushes its segment)
   stream_keys<K>(keys, n, [&](const K* kk, uint32_t valid, int nk) {
     uint32_t mm = 0;
 #pragma unroll
@@ -384,12 +399,13 @@ __global__ void __launch_bounds__(kSelBlock, 1) select_range_kernel(const K* key
       eq_hi += (v && key == hi) ? 1u : 0u;  // (discarded below when hi == lo)
       mm |= (v && (K)(key - lo1) < w) ? (1u << e) : 0u;
     }
-    seg_append<K>(kk, mm, nk, seg, fill, cand_a, cap_a, st);
+    seg_append<K>(kk, mm, nk, seg, fill, cand_a, cap_a, st, my_top);
   });
-  seg_flush<K>(seg, fill, cand_a, cap_a, st);
+  seg_flush<K>(seg, fill, cand_a, cap_a, st, my_top);
   if (below) atomicAdd(&s_cnt[0], below);
   if (eq_lo) atomicAdd(&s_cnt[1], eq_lo);
   if (eq_hi) atomicAdd(&s_cnt[2], eq_hi);
+  fold_counts(s_h, st, true);  // (its barrier also orders the count atomics above)
   __syncthreads();
   if (threadIdx.x == 0) {
     if (s_cnt[0]) atomicAdd(&st->below, (unsigned long long)s_cnt[0]);
@@ -418,7 +434,7 @@ __global__ void __launch_bounds__(kSelBlock, 1) select_range_kernel(const K* key
       mode = 1;
     }
     if (mode == 1) st->done = 1;
-    if (mode == 2) {  // the first step counts the candidates' top digit
+    if (mode == 2) {  // continue in the candidates: their top digit is picked below
       st->k = k - b - el;
       st->count = inside;
       st->cand_n[0] = inside;
@@ -430,7 +446,14 @@ __global__ void __launch_bounds__(kSelBlock, 1) select_range_kernel(const K* key
       st->overflow = 0;
     }
     st->cand_fill = 0;
-    st->ticket = 0;
+    s_mode = mode;
+  }
+  __syncthreads();
+  if (s_mode == 2) {
+    pick_bin<K>(st, st->hist, false, out);  // (resets the ticket and the counts)
+  } else {
+    if (threadIdx.x < 256) st->hist[threadIdx.x] = 0;
+    if (threadIdx.x == 0) st->ticket = 0;
   }
 }
 
