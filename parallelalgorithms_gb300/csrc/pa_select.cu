@@ -25,9 +25,10 @@
 //            the prefix (lane-banked shared counters), and the last CTA
 //            picks the bin.  A step whose digit is already decided (or
 //            whose answer is already written) returns at once.
-// A step may copy the keys sharing the prefix into the next candidate
-// buffer (input -> buffer A -> buffer B) when they fit it, and later steps
-// read only that buffer.  All state lives on the device, so the host
+// A step may copy the keys sharing the prefix into the other candidate
+// buffer (input -> A, A -> B, B -> A) when they fit it, and later steps read
+// only that buffer; once a step has copied few keys, its last CTA finishes
+// the remaining digits in shared memory.  All state lives on the device, so the host
 // enqueues key_bits / 8 + 3 launches and never waits between them.
 #include <cmath>
 
@@ -89,10 +90,11 @@ __device__ __forceinline__ bool matches(K key, unsigned long long prefix, uint32
 
 // Picks the bin of h (256 complete counts of the next digit over the keys
 // sharing the prefix) holding rank st->k and narrows the state to it (called
-// by every thread of one CTA of at least 256 threads).  `compacted`: this
-// step filled the next candidate buffer.
+// by every thread of one CTA of at least 256 threads).  `compacted_to`: the
+// candidate buffer (1: A, 2: B) this step filled, which becomes the source;
+// 0: none.
 template <typename K>
-__device__ void pick_bin(SelectState* st, const unsigned long long* h, bool compacted, K* out) {
+__device__ void pick_bin(SelectState* st, const unsigned long long* h, uint32_t compacted_to, K* out) {
   constexpr uint32_t W = 8u * sizeof(K);
   __shared__ unsigned long long s_tot[8];
   const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
@@ -101,7 +103,7 @@ __device__ void pick_bin(SelectState* st, const unsigned long long* h, bool comp
   // thread reading st->k after the update would see the narrowed rank and
   // could wrongly match a lower bin as well.
   const unsigned long long k = st->k, prefix0 = st->prefix;
-  const uint32_t bits0 = st->prefix_bits, src0 = st->src;
+  const uint32_t bits0 = st->prefix_bits;
   const unsigned long long c = t < 256 ? ld_relaxed_gpu(&h[t]) : 0ull;
   unsigned long long incl = c;  // inclusive scan of the 256 counts
 #pragma unroll
@@ -121,9 +123,9 @@ __device__ void pick_bin(SelectState* st, const unsigned long long* h, bool comp
       st->prefix_bits = bits0 + 8;
       st->k = k - excl;
       st->count = c;
-      if (compacted) {
-        st->cand_n[src0] = ld_relaxed_gpu(&st->cand_fill);  // filled by every CTA's atomics
-        st->src = src0 + 1;
+      if (compacted_to) {
+        st->cand_n[compacted_to - 1] = ld_relaxed_gpu(&st->cand_fill);  // filled by every CTA's atomics
+        st->src = compacted_to;
       }
       st->cand_fill = 0;
       if (bits0 + 8 == W) {
@@ -450,10 +452,90 @@ __global__ void __launch_bounds__(kSelBlock, 1) select_range_kernel(const K* key
   }
   __syncthreads();
   if (s_mode == 2) {
-    pick_bin<K>(st, st->hist, false, out);  // (resets the ticket and the counts)
+    pick_bin<K>(st, st->hist, 0u, out);  // (resets the ticket and the counts)
   } else {
     if (threadIdx.x < 256) st->hist[threadIdx.x] = 0;
     if (threadIdx.x == 0) st->ticket = 0;
+  }
+}
+
+// When the keys this step compacted are few (at most kFinishKeys), the
+// step's last CTA finishes the select itself: it loads the ones sharing the
+// new prefix from the buffer just written (other CTAs wrote it: L2 reads)
+// into shared memory and narrows their remaining digits there, so the later
+// step launches return at once.  Called by every thread of the last CTA
+// after pick_bin.
+template <typename K>
+constexpr uint32_t kFinishKeys = (uint32_t)(kStreamSmem / sizeof(K));
+template <typename K>
+__device__ void finish_in_cta(SelectState* st, const K* buf, K* s_keys, K* out) {
+  constexpr uint32_t W = 8u * sizeof(K);
+  __shared__ uint32_t s_fc[256];
+  __shared__ uint32_t s_n;
+  __shared__ unsigned long long s_pref, s_rank;
+  __shared__ bool s_go;
+  const uint32_t tid = threadIdx.x;
+  if (tid == 0) {
+    const uint32_t src = st->src;
+    s_go = !st->done && src != 0 && st->cand_n[src - 1] <= (unsigned long long)kFinishKeys<K>;
+    s_n = 0;
+    s_pref = st->prefix;
+    s_rank = st->k;
+  }
+  __syncthreads();
+  if (!s_go) return;
+  uint32_t pbits = st->prefix_bits;
+  const unsigned long long prefix = s_pref;
+  const uint32_t len = (uint32_t)st->cand_n[st->src - 1];
+  for (uint32_t i = tid; i < len; i += kSelBlock) {
+    const K key = __ldcg(&buf[i]);
+    if (matches(key, prefix, pbits)) s_keys[atomicAdd(&s_n, 1u)] = key;
+  }
+  __syncthreads();
+  const uint32_t m = s_n;
+  for (; pbits < W; pbits += 8) {
+    const uint32_t shift = W - 8u - pbits;
+    for (uint32_t i = tid; i < 256u; i += kSelBlock) s_fc[i] = 0;
+    __syncthreads();
+    const unsigned long long p = s_pref;
+    for (uint32_t j = tid; j < m; j += kSelBlock)
+      if (matches(s_keys[j], p, pbits)) atomicAdd(&s_fc[(uint32_t)(s_keys[j] >> shift) & 255u], 1u);
+    __syncthreads();
+    if (tid < 32) {  // lane l owns bins [8l, 8l + 8)
+      const uint32_t lane = tid;
+      uint32_t c[8], sum = 0;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        c[i] = s_fc[8 * lane + i];
+        sum += c[i];
+      }
+      uint32_t incl = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+      }
+      const unsigned long long rk = s_rank, pref = s_pref;
+      __syncwarp();  // every lane has read the target before one lane narrows it
+      uint32_t acc = incl - sum;
+      if ((unsigned long long)acc <= rk && rk < (unsigned long long)incl) {
+        for (int i = 0; i < 8; ++i) {
+          if (rk < (unsigned long long)(acc + c[i])) {
+            s_pref = (pref << 8) | (8u * lane + (uint32_t)i);
+            s_rank = rk - acc;
+            break;
+          }
+          acc += c[i];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    *out = (K)s_pref;
+    st->prefix = s_pref;
+    st->prefix_bits = W;
+    st->done = 1;
   }
 }
 
@@ -478,11 +560,12 @@ __global__ void __launch_bounds__(kSelBlock, 1) select_step_kernel(const K* keys
   const uint32_t src = st->src;
   const K* in = src == 0 ? keys : src == 1 ? cand_a : cand_b;
   const size_t len = src == 0 ? n : (size_t)st->cand_n[src - 1];
-  K* dst = src == 0 ? cand_a : cand_b;
-  const size_t cap = src == 0 ? cap_a : cap_b;
-  // compaction goes one buffer further each time, so it never overlaps its
-  // own source
-  const bool compact = src < 2 && st->count <= (unsigned long long)cap;
+  // compaction goes to the other candidate buffer (the input to A, A to B,
+  // B to A), so it never overlaps its own source
+  const uint32_t to = src == 1 ? 2u : 1u;
+  K* dst = to == 1 ? cand_a : cand_b;
+  const size_t cap = to == 1 ? cap_a : cap_b;
+  const bool compact = st->count <= (unsigned long long)cap;
   __syncthreads();
   const uint32_t warp = threadIdx.x >> 5;
   K* seg = reinterpret_cast<K*>(seg_smem) + (size_t)warp * kSegKeys<K>;
@@ -508,7 +591,8 @@ __global__ void __launch_bounds__(kSelBlock, 1) select_step_kernel(const K* keys
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  pick_bin<K>(st, st->hist, compact, out);
+  pick_bin<K>(st, st->hist, compact ? to : 0u, out);
+  if (compact) finish_in_cta<K>(st, dst, reinterpret_cast<K*>(seg_smem), out);
 }
 
 template <typename K>
