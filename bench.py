@@ -65,7 +65,75 @@ def parse_args():
     p.add_argument("--cpu-steps", type=int, default=5)
     p.add_argument("--no-extras", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    # profiling driver: runs one operation `--reps` times on device-resident
+    # seeded input and prints no JSON line (the commands in profiles/ use it)
+    p.add_argument("--profile-op", default=None,
+                   choices=["sort_u32", "sort_u32_host", "sort_u64", "sort_kv_u64", "sort_f32", "hist_u32",
+                            "select_u32", "sum_u32"])
+    p.add_argument("--reps", type=int, default=2)
+    p.add_argument("--dist", default="uniform", choices=["uniform", "presorted", "constant"])
     return p.parse_args()
+
+
+def profile_op(a) -> None:
+    """Runs one operation of the path `a.reps` times with nothing else on the
+    GPU, so that an ncu launch filter (-k regex:... -s <skip> -c <count>)
+    lands on known launches.  The seeded input is generated once and kept
+    device-resident.  Per sort: the workspace memset, one digit histogram,
+    one scan, one onesweep launch per key byte, one final copy.
+    `sort_u32_host` sorts a page-locked host copy through the C ABI instead
+    (the pipelined host-buffer path)."""
+    import torch
+
+    from parallelalgorithms_gb300 import _native, build, workloads
+    build.build()
+    P = ctypes.c_void_p
+    n = a.n
+    if a.profile_op in ("sort_kv_u64", "sort_u64"):
+        keys = workloads.uniform_u64(n)
+    elif a.profile_op == "sort_f32":
+        keys = workloads.normal_specials_f32(n).view(np.uint32)
+    elif a.dist == "presorted":
+        keys = workloads.presorted_u32(n)
+    elif a.dist == "constant":
+        keys = workloads.constant_u32(n)
+    else:
+        keys = workloads.uniform_u32(n)
+    src = torch.from_numpy(keys.view({4: np.int32, 8: np.int64}[keys.dtype.itemsize])).cuda()
+    k = torch.empty_like(src)
+    t = torch.empty_like(src)
+    v = tv = None
+    if a.profile_op == "sort_kv_u64":
+        v = torch.arange(n, dtype=torch.int32, device="cuda")
+        tv = torch.empty_like(v)
+    out = torch.zeros(256, dtype=torch.int64, device="cuda")
+    o = _native.opts(torch.cuda.current_stream().cuda_stream)
+    host_t = host = None
+    if a.profile_op == "sort_u32_host":
+        host_t = torch.empty(n, dtype=torch.int32, pin_memory=True)  # (kept alive for the view below)
+        host = host_t.numpy().view(np.uint32)
+    op = a.profile_op
+    for _ in range(a.reps):
+        k.copy_(src)
+        if op == "sort_u32_host":
+            np.copyto(host, keys)
+            _native.call("pa_sort_u32", P(host.ctypes.data), None, n, None)
+        elif op == "sort_u32":
+            _native.call("pa_sort_u32", P(k.data_ptr()), P(t.data_ptr()), n, o)
+        elif op == "sort_f32":
+            _native.call("pa_sort_f32", P(k.data_ptr()), P(t.data_ptr()), n, o)
+        elif op == "sort_u64":
+            _native.call("pa_sort_u64", P(k.data_ptr()), P(t.data_ptr()), n, o)
+        elif op == "sort_kv_u64":
+            _native.call("pa_sort_kv_u64", P(k.data_ptr()), P(v.data_ptr()), P(t.data_ptr()), P(tv.data_ptr()), n, o)
+        elif op == "hist_u32":
+            _native.call("pa_hist_byte_components_u32", P(k.data_ptr()), n, P(out.data_ptr()), o)
+        elif op == "select_u32":
+            _native.call("pa_select_u32", P(k.data_ptr()), n, n // 2, P(out.data_ptr()), o)
+        elif op == "sum_u32":
+            _native.call("pa_sum_u32", P(k.data_ptr()), n, P(out.data_ptr()), o)
+    torch.cuda.synchronize()
+    print(f"profile driver done: op={op} n={n} reps={a.reps}")
 
 
 # ---------------------------------------------------------------------------
@@ -221,23 +289,34 @@ def cpu_reference_sort(keys: np.ndarray, steps: int, warmup: int) -> dict:
             "ms": [t * 1e3 for t in times]}
 
 
+def workload_config(n: int, world: int) -> dict:
+    """The `config` both arms print (same workload, same keys)."""
+    return {"workload": f"LSD radix sort of {n} uniform uint32 keys (mt19937_64 seed 1234), 8-bit digits, 4 passes",
+            "keys_per_gpu": n, "key_type": "uint32", "distribution": "uniform mt19937_64(1234)", "digit_bits": 8,
+            "l2": "inputs (400 MB) larger than L2; no flush",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def reference_arm(args) -> None:
+    """The reference's own SortRadixPar on this host's cores.  Loads only the
+    CPU checkers under oracle/ (the compiled reference, or the restatement
+    where the reference could not be built); the GPU library is never
+    loaded, and the keys come from the reference benchmark's own recipe."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return
-    from parallelalgorithms_gb300 import build as pabuild
-    pabuild.build()
-    from parallelalgorithms_gb300 import workloads
-    keys = workloads.uniform_u32(args.n)
+    import oracle
+    from oracle import build as obuild
+    obuild.build_ref()
+    ref = oracle.ref()
+    keys = (ref if ref is not None else oracle.port()).gen_uniform_u32(args.n, 1234)
     cb = cpu_reference_sort(keys, args.steps, args.warmup)
     med_s = args.n / cb["value"]
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": med_s * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": cb["value"] / PUBLISHED_KEYS_PER_S, "vs_baseline_source": PUBLISHED_SOURCE,
             "dtype": "u32", "data": "synthetic",
-            "config": {"workload": f"LSD radix sort of {args.n} uniform uint32 keys, 8-bit digits",
-                       "keys": args.n, "key_type": "uint32", "distribution": "uniform mt19937_64(1234)",
-                       "l2": "inputs (400 MB) larger than L2"},
+            "config": workload_config(args.n, world),
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -370,14 +449,10 @@ def gb300_arm(args) -> None:
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": value / PUBLISHED_KEYS_PER_S, "vs_baseline_source": PUBLISHED_SOURCE,
             "dtype": "u32", "data": "synthetic",
-            "config": {"workload": f"LSD radix sort of {n} uniform uint32 keys (mt19937_64 seed 1234), "
-                                   "8-bit digits, 4 passes, device-resident",
-                       "keys_per_gpu": n, "key_type": "uint32", "digit_bits": 8,
-                       "l2": "inputs (400 MB) larger than L2; no flush",
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "step_timing": "CUDA events around each sort; input restored from a pristine device copy "
-                                      "before each step, outside the events",
-                       "wall_ms_per_step_incl_restore": wall * 1e3 / args.steps},
+            "config": workload_config(n, world),
+            "step_timing": {"how": "CUDA events around each device-resident sort; input restored from a pristine "
+                                   "device copy before each step, outside the events",
+                            "wall_ms_per_step_incl_restore": wall * 1e3 / args.steps},
             "roofline": roofline, "sort_roofline": whole, "e2e": e2e, "cpu_baseline": cpu,
             "gpu_launches": launches_per_step * args.steps, "clocks": sampler.summary(), "extras": extras,
         }
@@ -659,7 +734,9 @@ def run_extras(pa, lib, _native, workloads, n, stream, peak) -> dict:
 
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.profile_op:
+        profile_op(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         gb300_arm(args)

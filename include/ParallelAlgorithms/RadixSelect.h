@@ -1,7 +1,10 @@
 // Drop-in replacement for the reference's RadixSelect.h entry points (global
 // namespace, like the reference).  Returns the exact k-th smallest element
-// and, like the reference, leaves it at a[k].  The reference also rearranges
-// the rest of the range as it narrows; the GPU path leaves it unchanged.
+// and, like the reference, leaves it at a[k]: the GPU path swaps a[k] with the
+// first element of the range that holds the answer, so the range stays a
+// permutation of its input.  The reference rearranges the range further as
+// it narrows (its in-place partitioning); nothing else of the range is moved
+// here.
 #ifndef PA_DROPIN_RADIXSELECT_H
 #define PA_DROPIN_RADIXSELECT_H
 

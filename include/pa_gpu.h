@@ -155,9 +155,11 @@ int pa_start_of_bins_u32(const uint32_t* a, size_t n, size_t work_quanta, size_t
  * pa_select_radix_u32: the reference's contract, SelectRadix(a, start,
  *   length, k) (RadixSelect.h:139; SelectRadix(a, length, k) is start = 0,
  *   RadixSelect.h:157): the (k - start)-th smallest of a[start, start + length)
- *   with k an absolute index in that range, returned in *out AND stored to
- *   a[k].  The reference also rearranges the rest of the range; here the rest
- *   of `a` is left as it was.
+ *   with k an absolute index in that range, returned in *out AND left at
+ *   a[k]: a[k] is swapped with the first element of the range that holds the
+ *   answer, so the range stays a permutation of its input.  The reference
+ *   rearranges the range further (its in-place partitioning); here no other
+ *   element moves.
  */
 int pa_select_u32(const uint32_t* a, size_t n, size_t k, uint32_t* out, const pa_opts* opts);
 int pa_select_u64(const uint64_t* a, size_t n, size_t k, uint64_t* out, const pa_opts* opts);
@@ -173,6 +175,27 @@ int pa_select_radix_u32(uint32_t* a, size_t start, size_t length, size_t k, uint
  */
 int pa_sum_u32(const uint32_t* a, size_t n, uint64_t* out, const pa_opts* opts);
 int pa_sum_u64(const uint64_t* a, size_t n, uint64_t* out, const pa_opts* opts);
+
+/* Element kinds of the typed sums. */
+enum {
+  PA_ELEM_U8 = 0, PA_ELEM_I8 = 1, PA_ELEM_U16 = 2, PA_ELEM_I16 = 3, PA_ELEM_U32 = 4, PA_ELEM_I32 = 5,
+  PA_ELEM_U64 = 6, PA_ELEM_I64 = 7, PA_ELEM_F32 = 8, PA_ELEM_F64 = 9
+};
+/* *out = sum of a[0, n) with every element converted to a 64-bit integer
+ * first (unsigned kinds zero-extended, signed kinds sign-extended, float and
+ * double truncated toward zero), modulo 2^64: the two's-complement bits of
+ * the reference's template SumParallel<_Type>(in_array, l, r) -> long long
+ * (SumParallel.h:207-237), with a = in_array + l, n = r - l.  Float values
+ * outside the 64-bit range (undefined behaviour in the reference) saturate. */
+int pa_sum_typed(const void* a, size_t n, int elem_kind, uint64_t* out, const pa_opts* opts);
+/* Per-chunk sums: chunk_sums[i] = sum of a[i * chunk, min(n, (i + 1) * chunk))
+ * for the ceil(n / chunk) chunks, *out = their total, each modulo 2^64
+ * (elements widened as in pa_sum_typed).  Replaces the caller-buffer
+ * overloads SumParallelNonRecursive(in_array, l, r, sum_array,
+ * parallelThreshold) (SumParallel.h:419, :442), which leave each task's sum
+ * in sum_array, with chunk = parallelThreshold. */
+int pa_sum_chunked(const void* a, size_t n, int elem_kind, size_t chunk, uint64_t* chunk_sums, uint64_t* out,
+                   const pa_opts* opts);
 
 /* ---- batched segmented sort -----------------------------------------------
  * No reference counterpart (the reference sorts one array per call).  Sorts
@@ -282,6 +305,15 @@ int pa_sort_copy_u32(uint32_t* src, uint32_t* dst, size_t n, const pa_opts* opts
  * its serial in-place swap loop): here the whole array comes out sorted, the
  * GPU's cheapest way to partition around many k at once. */
 int pa_partition_radix_u32(uint32_t* a, size_t n, const size_t* k, size_t k_len, const pa_opts* opts);
+
+/* Failure-detection self-test (no reference counterpart; the reference has
+ * no waits that can run out).  Runs one onesweep digit pass of a small sort
+ * in which a tile's decoupled look-back polls a predecessor's status word
+ * that is never published, with the poll budget lowered to spin_limit, and
+ * returns what a sort whose wait ran out returns: PA_ERR_TIMEOUT (the
+ * expected result), with the device left usable.  The wait is bounded like
+ * every wait in this library; nothing faults or hangs. */
+int pa_selftest_wait_expiry(unsigned spin_limit);
 
 /* 256-bin histogram of (key >> shift) & 255 over 64-bit keys (no reference
  * counterpart; the 32-bit form is pa_hist_one_byte_u32). shift < 64. */

@@ -52,7 +52,15 @@ class _Port:
         h.pa_oracle_sum_u64.restype = ctypes.c_uint64
         h.pa_oracle_counting_sort_u8.argtypes = [_P, _SZ, _SZ]
         h.pa_oracle_partition_radix_u32.argtypes = [_P, _SZ, _P, _SZ]
+        h.pa_oracle_gen_uniform_u32.argtypes = [ctypes.c_uint64, _SZ, _P]
+        h.pa_oracle_gen_uniform_u32.restype = None
         self.h = h
+
+    def gen_uniform_u32(self, n: int, seed: int = 1234) -> np.ndarray:
+        """The reference benchmark's keys: (uint32)std::mt19937_64(seed)()."""
+        a = np.empty(n, np.uint32)
+        self.h.pa_oracle_gen_uniform_u32(seed, n, _p(a))
+        return a
 
     def sort(self, keys: np.ndarray, vals: np.ndarray | None = None, digit_bits: int = 8):
         """Returns sorted copies (keys, vals) -- SortRadixPar widened to
@@ -153,8 +161,12 @@ class _Ref:
         for f in ("pa_ref_sum_par_nonrec_u32", "pa_ref_sum_par_nonrec_u64", "pa_ref_sum_par_u64"):
             getattr(h, f).argtypes = [_P, _SZ, _SZ]
             getattr(h, f).restype = ctypes.c_ulonglong
-        h.pa_ref_sum_par_template_u32.argtypes = [_P, _SZ, _SZ]
-        h.pa_ref_sum_par_template_u32.restype = ctypes.c_longlong
+        for f in ("pa_ref_sum_par_template_u32", "pa_ref_sum_par_template_u8", "pa_ref_sum_par_template_i32",
+                  "pa_ref_sum_par_template_f32"):
+            getattr(h, f).argtypes = [_P, _SZ, _SZ]
+            getattr(h, f).restype = ctypes.c_longlong
+        h.pa_ref_sum_par_nonrec_array_u32.argtypes = [_P, _SZ, _SZ, _P, _SZ]
+        h.pa_ref_sum_par_nonrec_array_u32.restype = ctypes.c_ulonglong
         h.pa_ref_std_stable_sort_u64.argtypes = [_P, _SZ]
         h.pa_ref_std_stable_sort_f32_bits.argtypes = [_P, _SZ]
         h.pa_ref_std_stable_sort_kv_u64.argtypes = [_P, _P, _SZ]
@@ -163,7 +175,15 @@ class _Ref:
         h.pa_ref_merge_sort_hybrid_radix_u32.argtypes = [_P, _SZ, _SZ, _P, ctypes.c_int]
         h.pa_ref_preventative_adaptive_sort_u32.argtypes = [_P, _SZ]
         h.pa_ref_msd_radix_sort_u32.argtypes = [_P, _SZ]
+        h.pa_ref_gen_uniform_u32.argtypes = [ctypes.c_uint64, _SZ, _P]
+        h.pa_ref_gen_uniform_u32.restype = None
         self.h = h
+
+    def gen_uniform_u32(self, n: int, seed: int = 1234) -> np.ndarray:
+        """The reference benchmark's keys: (uint32)std::mt19937_64(seed)()."""
+        a = np.empty(n, np.uint32)
+        self.h.pa_ref_gen_uniform_u32(seed, n, _p(a))
+        return a
 
     def threads(self) -> int:
         return int(self.h.pa_ref_hardware_concurrency())
@@ -230,6 +250,21 @@ class _Ref:
 
     def sum_template_u32(self, a, l=0, r=None) -> int:
         return int(self.h.pa_ref_sum_par_template_u32(_p(a), l, a.size if r is None else r))
+
+    def sum_template(self, a, l=0, r=None) -> int:
+        """template SumParallel<_Type> (SumParallel.h:207) for uint8 / uint32 /
+        int32 / float32 arrays."""
+        f = {np.dtype(np.uint8): self.h.pa_ref_sum_par_template_u8, np.dtype(np.uint32): self.h.pa_ref_sum_par_template_u32,
+             np.dtype(np.int32): self.h.pa_ref_sum_par_template_i32,
+             np.dtype(np.float32): self.h.pa_ref_sum_par_template_f32}[a.dtype]
+        return int(f(_p(a), l, a.size if r is None else r))
+
+    def sum_nonrec_array(self, a, l, r, threshold):
+        """SumParallelNonRecursive(a, l, r, sum_array, threshold): (total, sum_array)."""
+        tasks = (r - l + threshold - 1) // threshold
+        arr = np.zeros(max(tasks, 1), np.uint64)
+        total = int(self.h.pa_ref_sum_par_nonrec_array_u32(_p(a), l, r, _p(arr), threshold))
+        return total, arr[:tasks]
 
     def counting_sort_u8(self, a: np.ndarray) -> np.ndarray:
         c = np.ascontiguousarray(a).copy()

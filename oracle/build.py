@@ -6,12 +6,13 @@
    unchanged with oracle/ref_capi.cpp, the TBB stand-in (oracle/tbb_shim) and
    the Copy.h stand-in (oracle/ref_stub), g++.
 
-The reference headers are read from /root/reference when it exists; the
-include closure of ref_capi.cpp is also staged (unmodified, never committed:
-oracle/_ref/ is git-ignored) in oracle/_ref/src/, so that a machine without
-/root/reference (such as an aarch64 host, on which x86 objects cannot run)
-rebuilds the same reference code from there.  Nothing here is run by
-the product path.
+The reference headers are read from the reference checkout: the directory
+named by the environment variable PA_REFERENCE_DIR, else `reference` beside
+this repository's root.  The include closure of ref_capi.cpp is also staged
+(unmodified, never committed: oracle/_ref/ is git-ignored) in
+oracle/_ref/src/, so that a machine without the checkout (such as an aarch64
+host, on which x86 objects cannot run) rebuilds the same reference code from
+there.  Nothing here is run by the product path.
 """
 from __future__ import annotations
 
@@ -24,7 +25,7 @@ from pathlib import Path
 ORACLE = Path(__file__).resolve().parent
 REF_OUT = ORACLE / "_ref"
 REF_SRC_STAGE = REF_OUT / "src"
-REFERENCE = Path(os.environ.get("PA_REFERENCE_DIR", "/root/reference"))
+REFERENCE = Path(os.environ.get("PA_REFERENCE_DIR", str(ORACLE.parent.parent / "reference")))
 
 ORACLE_LIB = ORACLE / "libpa_oracle.so"
 REF_LIB = REF_OUT / "libpa_ref.so"
@@ -72,7 +73,7 @@ def _closure(root_files: list[Path], search: list[Path]) -> set[str]:
 
 def _stage_reference() -> Path | None:
     """Returns the directory to compile the reference from, staging it when
-    /root/reference is available."""
+    the reference checkout is available."""
     if REFERENCE.is_dir():
         names = _closure([ORACLE / "ref_capi.cpp"], [ORACLE / "ref_stub", REFERENCE])
         REF_SRC_STAGE.mkdir(parents=True, exist_ok=True)

@@ -411,3 +411,33 @@ void pa_oracle_partition_radix_u32(uint32_t* a, size_t n, const size_t* k, size_
   if (n == 0 || klen == 0) return;
   partition_inner(a, 0, n, 24, k, 0, klen);
 }
+
+/* The reference benchmark's keys (ParallelAlgorithms.cpp:91, 112-115):
+ * low 32 bits of each draw of a 64-bit Mersenne Twister seeded with `seed`
+ * (std::mt19937_64).  The generator is the published MT19937-64 of
+ * Matsumoto and Nishimura (2000): 312 words of state, twist at 156, tempering
+ * shifts 29 / 17 / 37 / 43, initialisation multiplier 6364136223846793005.
+ * Lets the CPU baseline make its input without the GPU library. */
+void pa_oracle_gen_uniform_u32(uint64_t seed, size_t n, uint32_t* out) {
+  enum { NN = 312, MM = 156 };
+  const uint64_t matrix_a = 0xB5026F5AA96619E9ull, upper = 0xFFFFFFFF80000000ull, lower = 0x7FFFFFFFull;
+  uint64_t mt[NN];
+  mt[0] = seed;
+  for (int i = 1; i < NN; i++) mt[i] = 6364136223846793005ull * (mt[i - 1] ^ (mt[i - 1] >> 62)) + (uint64_t)i;
+  int idx = NN;
+  for (size_t k = 0; k < n; k++) {
+    if (idx >= NN) {
+      for (int i = 0; i < NN; i++) {
+        const uint64_t x = (mt[i] & upper) | (mt[(i + 1) % NN] & lower);
+        mt[i] = mt[(i + MM) % NN] ^ (x >> 1) ^ ((x & 1u) ? matrix_a : 0u);
+      }
+      idx = 0;
+    }
+    uint64_t y = mt[idx++];
+    y ^= (y >> 29) & 0x5555555555555555ull;
+    y ^= (y << 17) & 0x71D67FFFEDA60000ull;
+    y ^= (y << 37) & 0xFFF7EEE000000000ull;
+    y ^= y >> 43;
+    out[k] = (uint32_t)y;
+  }
+}

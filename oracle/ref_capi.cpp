@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cstring>
 #include <algorithm>
+#include <random>
 #include <thread>
 #include <vector>
 
@@ -29,6 +30,14 @@ unsigned long long physical_memory_total_in_megabytes() { return 0; }
 extern "C" {
 
 int pa_ref_hardware_concurrency(void) { return tbb::info::default_concurrency(); }
+
+// The reference benchmark's input recipe (ParallelAlgorithms.cpp:91,
+// 112-115): std::mt19937_64(seed), key = low 32 bits of each draw.  Lets the
+// timed reference run make its own input without loading the GPU library.
+void pa_ref_gen_uniform_u32(uint64_t seed, size_t n, uint32_t* out) {
+  std::mt19937_64 g(seed);
+  for (size_t i = 0; i < n; ++i) out[i] = (uint32_t)g();
+}
 
 // RadixSortLsdParallel.h:367 SortRadixPar(a, tmp_work_buff, a_size)
 void pa_ref_sort_radix_par_u32(unsigned* a, unsigned* tmp, size_t n) {
@@ -131,6 +140,23 @@ unsigned long long pa_ref_sum_par_u64(unsigned long long* a, size_t l, size_t r)
 // SumParallel.h:207 template SumParallel<unsigned>(a, l, r) -> long long
 long long pa_ref_sum_par_template_u32(unsigned* a, size_t l, size_t r) {
   return ParallelAlgorithms::SumParallel(a, l, r);
+}
+
+// The same template over other element types: unsigned char (the call of
+// SumBenchmark.cpp:101), int and float.
+long long pa_ref_sum_par_template_u8(unsigned char* a, size_t l, size_t r) {
+  return ParallelAlgorithms::SumParallel(a, l, r);
+}
+long long pa_ref_sum_par_template_i32(int* a, size_t l, size_t r) { return ParallelAlgorithms::SumParallel(a, l, r); }
+long long pa_ref_sum_par_template_f32(float* a, size_t l, size_t r) {
+  return ParallelAlgorithms::SumParallel(a, l, r);
+}
+
+// SumParallel.h:419 SumParallelNonRecursive(unsigned[], l, r, sum_array,
+// parallelThreshold): per-task sums left in sum_array.
+unsigned long long pa_ref_sum_par_nonrec_array_u32(unsigned* a, size_t l, size_t r, unsigned long long* sum_array,
+                                                   size_t threshold) {
+  return ParallelAlgorithms::SumParallelNonRecursive(a, l, r, sum_array, threshold);
 }
 
 // CountingSortParallel.h:81 counting_sort_parallel(a, a_size): byte array

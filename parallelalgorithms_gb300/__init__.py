@@ -17,8 +17,9 @@ Reference entry points mirrored here (file:line within the reference):
   HistogramByteComponentsQCPar         HistogramParallel.h:444
   ComputeStartOfBinsPar                RadixSortLsdParallel.h:108
   SelectRadix                          RadixSelect.h:139, :157
-  SumParallelNonRecursive              SumParallel.h:261, :285
+  SumParallelNonRecursive              SumParallel.h:261, :285, :419, :442
   SumParallel                          SumParallel.h:162, :207
+  SumParallelNonRecursiveBuffered(Locally), SumNonRecursive  SumParallel.h:309-416, :240
 """
 from __future__ import annotations
 
@@ -34,6 +35,7 @@ __all__ = [
     "RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase_DeRandomize",
     "HistogramByteComponentsParallel", "HistogramOneByteComponentParallel", "HistogramByteComponentsQCPar",
     "ComputeStartOfBinsPar", "SelectRadix", "SumParallelNonRecursive", "SumParallel",
+    "SumParallelNonRecursiveBufferedLocally", "SumParallelNonRecursiveBuffered", "SumNonRecursive",
     "counting_sort_parallel", "counting_sort_parallel_inner", "PartitionRadix",
     "parallel_merge_sort_hybrid_radix", "parallel_linear_in_place_preventative_adaptive_sort",
     "parallel_hybrid_inplace_msd_radix_sort",
@@ -55,7 +57,8 @@ def _info(x):
         if not x.is_contiguous():
             raise ValueError("tensor must be contiguous")
         dt = {torch.int32: np.uint32, torch.int64: np.uint64, torch.uint8: np.uint8,
-              torch.float32: np.float32}.get(x.dtype)
+              torch.float32: np.float32, torch.int8: np.int8, torch.int16: np.int16,
+              torch.float64: np.float64}.get(x.dtype)
         if hasattr(torch, "uint32") and x.dtype == torch.uint32:
             dt = np.uint32
         if hasattr(torch, "uint64") and x.dtype == torch.uint64:
@@ -231,8 +234,9 @@ def ComputeStartOfBinsPar(inArray, size: int, workQuanta: int, numberOfQuantas: 
 def SelectRadix(a, *args) -> int:
     """RadixSelect.h:157 SelectRadix(a, length, k) and :139 SelectRadix(a,
     start, length, k): the k-th smallest (k absolute, 0-based) of
-    a[start, start + length); like the reference it also stores the result
-    to a[k].  The rest of `a` is left as it was."""
+    a[start, start + length); like the reference it leaves the result at
+    a[k], by swapping a[k] with the first element of the range that holds
+    it, so `a` stays a permutation of its input."""
     if len(args) == 2:
         start, (length, k) = 0, args
     elif len(args) == 3:
@@ -269,20 +273,74 @@ def _sum(in_array, l: int, r: int) -> int:
     return int(out[0])
 
 
-def SumParallelNonRecursive(in_array, l: int, r: int, parallelThreshold: int = 16 * 1024) -> int:
+# element kinds of pa_sum_typed (PA_ELEM_* in include/pa_gpu.h)
+_ELEM_KIND = {np.dtype(np.uint8): 0, np.dtype(np.int8): 1, np.dtype(np.uint16): 2, np.dtype(np.int16): 3,
+              np.dtype(np.uint32): 4, np.dtype(np.int32): 5, np.dtype(np.uint64): 6, np.dtype(np.int64): 7,
+              np.dtype(np.float32): 8, np.dtype(np.float64): 9}
+
+
+def _elem(in_array) -> tuple[int, int]:
+    dt = _info(in_array)[2]
+    if dt not in _ELEM_KIND:
+        raise TypeError(f"no sum for element type {dt}")
+    return _ELEM_KIND[dt], dt.itemsize
+
+
+def _signed64(v: int) -> int:
+    return v - (1 << 64) if v >= (1 << 63) else v
+
+
+def SumParallelNonRecursive(in_array, l: int, r: int, sum_array=None, parallelThreshold: int = 16 * 1024) -> int:
     """SumParallel.h:261 (unsigned[]) and :285 (unsigned long long[]): sum of
-    in_array[l, r), r exclusive, modulo 2^64, as an unsigned 64-bit value."""
-    return _sum(in_array, l, r)
+    in_array[l, r), r exclusive, modulo 2^64, as an unsigned 64-bit value.
+    With `sum_array` (a uint64 array of ceil((r - l) / parallelThreshold)
+    entries, or an int in its place, which is then taken as the threshold),
+    the caller-buffer overloads :419, :442: sum_array[i] receives the sum of
+    the i-th parallelThreshold-element chunk."""
+    if isinstance(sum_array, (int, np.integer)):
+        sum_array, parallelThreshold = None, int(sum_array)
+    if sum_array is None:
+        return _sum(in_array, l, r)
+    kind, isz = _elem(in_array)
+    n = max(0, r - l)
+    need = -(-n // parallelThreshold)
+    if _info(sum_array)[1] < need:
+        raise ValueError(f"sum_array holds fewer than the {need} chunk sums")
+    out = np.zeros(1, np.uint64)
+    call("pa_sum_chunked", _offset(in_array, l, isz), n, kind, parallelThreshold, _ptr(sum_array),
+         ctypes.c_void_p(out.ctypes.data), _opts(in_array, sum_array))
+    return int(out[0])
 
 
 def SumParallel(in_array, l: int, r: int, parallelThreshold: int = 16 * 1024) -> int:
     """SumParallel.h:162 (unsigned long long[] -> unsigned long long) and the
-    template :207 (other element types -> long long, i.e. the same 64 bits
-    read as signed)."""
-    v = _sum(in_array, l, r)
-    if _kind(_info(in_array)[2]) == "u64":
-        return v
-    return v - (1 << 64) if v >= (1 << 63) else v
+    template :207 (any other element type -> long long): every element is
+    converted to a 64-bit integer (floats truncated toward zero) and summed
+    modulo 2^64; the template's result is those 64 bits read as signed.
+    Tensors of torch.int32 / int64 hold unsigned keys in this package and are
+    summed as such."""
+    kind, isz = _elem(in_array)
+    out = np.zeros(1, np.uint64)
+    call("pa_sum_typed", _offset(in_array, l, isz), max(0, r - l), kind, ctypes.c_void_p(out.ctypes.data),
+         _opts(in_array))
+    v = int(out[0])
+    return v if kind == _ELEM_KIND[np.dtype(np.uint64)] else _signed64(v)
+
+
+def SumParallelNonRecursiveBufferedLocally(in_array, l: int, r: int, parallelThreshold: int = 16 * 1024) -> int:
+    """SumParallel.h:309, :337: the same sum as SumParallelNonRecursive (the
+    reference's variant differs only in how each CPU task reads its chunk)."""
+    return _sum(in_array, l, r)
+
+
+def SumParallelNonRecursiveBuffered(in_array, l: int, r: int, parallelThreshold: int = 16 * 1024) -> int:
+    """SumParallel.h:366, :393: the same sum as SumParallelNonRecursive."""
+    return _sum(in_array, l, r)
+
+
+def SumNonRecursive(in_array, l: int, r: int, parallelThreshold: int = 128 * 1024) -> int:
+    """SumParallel.h:240 (unsigned long long[]): the same sum."""
+    return _sum(in_array, l, r)
 
 
 def sum_u64(a) -> int:

@@ -55,6 +55,8 @@ SIGNATURES: dict[str, list] = {
     "pa_select_radix_u32": [_P, _SZ, _SZ, _SZ, _P, _O],
     "pa_sum_u32": [_P, _SZ, _P, _O],
     "pa_sum_u64": [_P, _SZ, _P, _O],
+    "pa_sum_typed": [_P, _SZ, ctypes.c_int, _P, _O],
+    "pa_sum_chunked": [_P, _SZ, ctypes.c_int, _SZ, _P, _P, _O],
     "pa_segsort_plan_create": [_P, _SZ, ctypes.POINTER(SegSortConfig), ctypes.POINTER(ctypes.c_void_p)],
     "pa_segsort_plan_run": [_P, _P, _P, _O],
     "pa_segsort_plan_sync": [_P, _P],
@@ -68,6 +70,7 @@ SIGNATURES: dict[str, list] = {
     "pa_server_stats": [_P, _P, ctypes.c_int],
     "pa_server_destroy": [_P],
     "pa_hist_one_byte_u64": [_P, _SZ, _U, _P, _O],
+    "pa_selftest_wait_expiry": [_U],
     "pa_stream_check": [_P],
     "pa_device_available": [],
     "pa_release_workspaces": [],

@@ -12,8 +12,12 @@
 // registers, which is what a streaming read needs to reach HBM bandwidth.
 //
 // Every wait is bounded: a wait that gives up raises DEVERR_TMA_TIMEOUT in
-// *err and that thread stops streaming (its CTA's result is then invalid,
-// and the call reports the error).
+// *err and stops the streaming (the CTA's result is then invalid, and the
+// call reports the error).  A consumer warp leaves as a whole (so that no lane
+// is left alone in a warp-collective `consume`), the producer stops issuing
+// copies, and before the CTA exits the producer waits (bounded again) for the
+// copies it issued into stages that no consumer has waited out, so that no
+// copy lands in shared memory after the CTA is gone.
 #pragma once
 
 #include "pa_common.cuh"
@@ -62,6 +66,7 @@ __device__ __forceinline__ void bulk_stream(const void* src, size_t bytes, unsig
   const unsigned char* s8 = static_cast<const unsigned char*>(src);
   if (warp == kConsumerWarps) {
     if (lane == 0) {  // producer
+      size_t issued = 0;
       for (size_t j = 0; j < mine; ++j) {
         const uint32_t s = (uint32_t)(j % STAGES);
         if (j >= (size_t)STAGES && !mbar_wait_bounded(&empty[s], (uint32_t)((j / STAGES) - 1) & 1u, err)) break;
@@ -69,14 +74,21 @@ __device__ __forceinline__ void bulk_stream(const void* src, size_t bytes, unsig
         const uint32_t len = (uint32_t)min((size_t)CHUNK, bytes - off);
         mbar_arrive_expect_tx(&full[s], len);
         bulk_load_g2s(ring + (size_t)s * CHUNK, s8 + off, len, &full[s]);
+        issued = j + 1;
       }
+      // Only the last STAGES issued copies can still be in flight (an earlier
+      // stage was reused after its chunk was consumed); wait for their
+      // phases, which returns at once for every copy that has landed.
+      for (size_t j = issued > (size_t)STAGES ? issued - STAGES : 0; j < issued; ++j)
+        if (!mbar_wait_bounded(&full[j % STAGES], (uint32_t)(j / STAGES) & 1u, err)) break;
     }
   } else {  // consumers
     for (size_t j = 0; j < mine; ++j) {
       const uint32_t s = (uint32_t)(j % STAGES);
       const size_t off = (blockIdx.x + j * g) * (size_t)CHUNK;
       const uint32_t len = (uint32_t)min((size_t)CHUNK, bytes - off);
-      if (!mbar_wait_bounded(&full[s], (uint32_t)(j / STAGES) & 1u, err)) break;
+      const bool landed = mbar_wait_bounded(&full[s], (uint32_t)(j / STAGES) & 1u, err);
+      if (!__all_sync(0xFFFFFFFFu, landed)) break;  // the whole warp leaves together
       consume(reinterpret_cast<const uint4*>(ring + (size_t)s * CHUNK), len / 16u);
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);

@@ -622,10 +622,14 @@ int select_impl(const void* a, size_t n, size_t k, int kb, void* out, const pa_o
 // ---------------------------------------------------------------------------
 // Sum
 // ---------------------------------------------------------------------------
-int sum_impl(const void* a, size_t n, int kb, uint64_t* out, const pa_opts* opts) {
+int sum_impl(const void* a, size_t n, int elem_kind, uint64_t* out, const pa_opts* opts, size_t chunk = 0,
+             uint64_t* chunk_sums = nullptr) {
   if (int rc = check_opts(opts)) return rc;
+  const int kb = sum_elem_bytes(elem_kind);
+  if (kb == 0) return set_error(PA_ERR_ARG, "unknown element kind %d", elem_kind);
   if (!out) return set_error(PA_ERR_ARG, "out is NULL");
   if (n && !a) return set_error(PA_ERR_ARG, "input is NULL");
+  if (chunk_sums && chunk == 0) return set_error(PA_ERR_ARG, "chunk is 0");
   if (int rc = device_ready()) return rc;
   std::lock_guard<std::mutex> lock(g_mu);
   cudaStream_t stream = stream_of(opts);
@@ -633,15 +637,20 @@ int sum_impl(const void* a, size_t n, int kb, uint64_t* out, const pa_opts* opts
   if (int rc = get_workspace(stream, &ws)) return rc;
   const bool in_dev = is_device_ptr(a);
   const bool out_dev = is_device_ptr(out);
+  const size_t nchunks = chunk_sums ? ceil_div(n, chunk) : 0;
+  const bool sums_dev = chunk_sums && is_device_ptr(chunk_sums);
   const void* d_in = nullptr;
   unsigned long long* partials = nullptr;
   uint32_t* ticket = nullptr;
   unsigned long long* d_out = nullptr;
+  unsigned long long* d_sums = nullptr;
   auto layout = [&](Carve& c) {
     d_in = in_dev ? a : c.take<char>(n * kb);
     partials = c.take<unsigned long long>(sum_partials_needed());
     ticket = c.take<uint32_t>(1);
     d_out = out_dev ? reinterpret_cast<unsigned long long*>(out) : c.take<unsigned long long>(1);
+    if (chunk_sums)
+      d_sums = sums_dev ? reinterpret_cast<unsigned long long*>(chunk_sums) : c.take<unsigned long long>(nchunks);
   };
   Carve m{nullptr};
   layout(m);
@@ -649,10 +658,18 @@ int sum_impl(const void* a, size_t n, int kb, uint64_t* out, const pa_opts* opts
   Carve r{ws->dev};
   layout(r);
   if (!in_dev && n) PA_CUDA(cudaMemcpyAsync(const_cast<void*>(d_in), a, n * kb, cudaMemcpyHostToDevice, stream));
-  PA_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream));
-  PA_CUDA(launch_sum(d_in, n, kb, partials, ticket, d_out, ws->err, stream));
+  if (chunk_sums) {
+    // per-chunk sums (the reference's caller-provided sum_array) and their total
+    PA_CUDA(cudaMemsetAsync(d_out, 0, sizeof(uint64_t), stream));
+    PA_CUDA(launch_sum_chunks(d_in, n, elem_kind, chunk, d_sums, d_out, stream));
+    if (!sums_dev && nchunks)
+      PA_CUDA(cudaMemcpyAsync(chunk_sums, d_sums, nchunks * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+  } else {
+    PA_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream));
+    PA_CUDA(launch_sum(d_in, n, elem_kind, partials, ticket, d_out, ws->err, stream));
+  }
   if (!out_dev) PA_CUDA(cudaMemcpyAsync(out, d_out, sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
-  return finish(ws, stream, opts && opts->async_device && in_dev && out_dev);
+  return finish(ws, stream, opts && opts->async_device && in_dev && out_dev && (!chunk_sums || sums_dev));
 }
 
 }  // namespace
@@ -1015,24 +1032,116 @@ int pa_select_u64(const uint64_t* a, size_t n, size_t k, uint64_t* out, const pa
 }
 
 int pa_select_radix_u32(uint32_t* a, size_t start, size_t length, size_t k, uint32_t* out, const pa_opts* opts) {
+  if (int rc = check_opts(opts)) return rc;
   if (!a || !out) return set_error(PA_ERR_ARG, "NULL buffer");
   if (length == 0 || k < start || k - start >= length)
     return set_error(PA_ERR_ARG, "k = %zu is outside [start, start + length) = [%zu, %zu)", k, start, start + length);
-  uint32_t v = 0;
-  int rc = select_impl(a + start, length, k - start, 4, &v, opts);
-  if (rc != PA_OK) return rc;
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
   cudaStream_t stream = stream_of(opts);
-  PA_CUDA(cudaMemcpyAsync(a + k, &v, sizeof(v), cudaMemcpyDefault, stream));
-  PA_CUDA(cudaMemcpyAsync(out, &v, sizeof(v), cudaMemcpyDefault, stream));
-  PA_CUDA(cudaStreamSynchronize(stream));
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+  uint32_t* base = a + start;
+  const size_t n = length, kk = k - start;
+  const bool in_dev = is_device_ptr(base);
+  const bool out_dev = is_device_ptr(out);
+  const size_t cand_cap = n / 4 + 1024;
+  uint32_t* d_in = nullptr;
+  void *cand = nullptr, *work = nullptr;
+  uint32_t* d_val = nullptr;
+  unsigned long long* d_idx = nullptr;
+  auto layout = [&](Carve& c) {
+    d_in = in_dev ? base : c.take<uint32_t>(n);
+    cand = c.take<char>(cand_cap * 4);
+    work = c.take<char>(select_state_bytes());
+    d_val = c.take<uint32_t>(2);
+    d_idx = c.take<unsigned long long>(1);
+  };
+  Carve m{nullptr};
+  layout(m);
+  if (int rc = ensure_dev(ws, stream, m.off)) return rc;
+  Carve r{ws->dev};
+  layout(r);
+  if (!in_dev) PA_CUDA(cudaMemcpyAsync(d_in, base, n * 4, cudaMemcpyHostToDevice, stream));
+  PA_CUDA(launch_select(d_in, n, kk, 4, cand, cand_cap, work, d_val, ws->err, stream));
+  // The reference rearranges the range and leaves the answer at a[k]; here
+  // the answer is swapped with a[k] from the first place that holds it, so
+  // the range stays a permutation of its input.
+  PA_CUDA(launch_find_key(d_in, n, kk, d_val, d_idx, stream));
+  if (in_dev) PA_CUDA(launch_swap_key(d_in, n, kk, d_idx, stream));
+  PA_CUDA(cudaMemcpyAsync(out, d_val, 4, out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream));
+  unsigned long long idx = n;
+  if (!in_dev) PA_CUDA(cudaMemcpyAsync(&idx, d_idx, sizeof(idx), cudaMemcpyDeviceToHost, stream));
+  const int rc = finish(ws, stream, in_dev && out_dev && opts && opts->async_device);
+  if (rc != PA_OK) return rc;
+  if (!in_dev && idx < n && idx != kk) std::swap(base[idx], base[kk]);
   return PA_OK;
 }
 
+int pa_selftest_wait_expiry(unsigned spin_limit) {
+  if (spin_limit == 0) return set_error(PA_ERR_ARG, "spin_limit must be positive");
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t stream = 0;
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+  // Two tiles of keys; the one CTA launched takes ticket 1, so its look-back
+  // polls tile 0's status word, which no CTA ever publishes.
+  const size_t n = 2 * onesweep_tile_keys(4, false);
+  uint32_t *keys = nullptr, *tmp = nullptr, *ticket = nullptr;
+  unsigned long long* bin_start = nullptr;
+  char* status = nullptr;
+  SortCtrl* ctrl = nullptr;
+  auto layout = [&](Carve& c) {
+    keys = c.take<uint32_t>(n);
+    tmp = c.take<uint32_t>(n);
+    bin_start = c.take<unsigned long long>(256);
+    status = c.take<char>(2 * 256 * onesweep_status_bytes(n));
+    ticket = c.take<uint32_t>(1);
+    ctrl = c.take<SortCtrl>(1);  // all zero: pass 0 runs, keys -> tmp
+  };
+  Carve m{nullptr};
+  layout(m);
+  if (int rc = ensure_dev(ws, stream, m.off)) return rc;
+  Carve r{ws->dev};
+  layout(r);
+  static const uint32_t kTicket = 1;
+  PA_CUDA(cudaMemsetAsync(ws->dev, 0, r.off, stream));
+  PA_CUDA(cudaMemcpyAsync(ticket, &kTicket, sizeof(kTicket), cudaMemcpyHostToDevice, stream));
+  OnesweepArgs a{};
+  a.keys_a = keys;
+  a.keys_b = tmp;
+  a.n = n;
+  a.bin_start = bin_start;
+  a.status = status;
+  a.tile_counter = ticket;
+  a.ctrl = ctrl;
+  a.err = ws->err;
+  a.spin_limit = spin_limit;
+  a.max_ctas = 1;
+  PA_CUDA(launch_onesweep_pass(a, 4, false, stream));
+  return finish(ws, stream, false);
+}
+
 int pa_sum_u32(const uint32_t* a, size_t n, uint64_t* out, const pa_opts* opts) {
-  return sum_impl(a, n, 4, out, opts);
+  return sum_impl(a, n, kElemU32, out, opts);
 }
 int pa_sum_u64(const uint64_t* a, size_t n, uint64_t* out, const pa_opts* opts) {
-  return sum_impl(a, n, 8, out, opts);
+  return sum_impl(a, n, kElemU64, out, opts);
+}
+int pa_sum_typed(const void* a, size_t n, int elem_kind, uint64_t* out, const pa_opts* opts) {
+  return sum_impl(a, n, elem_kind, out, opts);
+}
+int pa_sum_chunked(const void* a, size_t n, int elem_kind, size_t chunk, uint64_t* chunk_sums, uint64_t* out,
+                   const pa_opts* opts) {
+  if (n && !chunk_sums) return set_error(PA_ERR_ARG, "chunk_sums is NULL");
+  if (n == 0) {
+    if (!out) return set_error(PA_ERR_ARG, "out is NULL");
+    const uint64_t zero = 0;
+    PA_CUDA(cudaMemcpy(out, &zero, sizeof(zero), cudaMemcpyDefault));
+    return PA_OK;
+  }
+  return sum_impl(a, n, elem_kind, out, opts, chunk, chunk_sums);
 }
 
 }  // extern "C"

@@ -95,6 +95,8 @@ struct OnesweepArgs {
   uint32_t* tile_counter;               // this pass's tile ticket
   const SortCtrl* ctrl;
   uint32_t* err;
+  uint32_t spin_limit = 0;  // look-back polls before a tile gives up; 0 = kSpinLimit
+  size_t max_ctas = 0;      // CTAs launched; 0 = one per tile (only the wait-expiry self-test sets it)
 };
 
 // Tile geometry chosen for (key_bytes, has_vals); the workspace is sized
@@ -170,12 +172,23 @@ cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32
                          const std::function<cudaError_t()>& mark = {});
 
 // ---- sum (pa_sum.cu) -------------------------------------------------------
-// out = sum of keys[0, n) modulo 2^64.  partials holds sum_partials_needed()
-// words and ticket one zeroed word; a bulk-copy wait that gives up raises a
-// bit in *err.
+// Element kinds of the sums (the values of pa_gpu.h's PA_ELEM_*).
+enum : int {
+  kElemU8 = 0, kElemI8 = 1, kElemU16 = 2, kElemI16 = 3, kElemU32 = 4, kElemI32 = 5,
+  kElemU64 = 6, kElemI64 = 7, kElemF32 = 8, kElemF64 = 9
+};
+// Bytes of one element of `elem_kind` (0 for an unknown kind).
+int sum_elem_bytes(int elem_kind);
+// out = sum of keys[0, n), each element widened to 64 bits, modulo 2^64.
+// partials holds sum_partials_needed() words and ticket one zeroed word; a
+// bulk-copy wait that gives up raises a bit in *err.
 size_t sum_partials_needed();
-cudaError_t launch_sum(const void* keys, size_t n, int key_bytes, unsigned long long* partials, uint32_t* ticket,
+cudaError_t launch_sum(const void* keys, size_t n, int elem_kind, unsigned long long* partials, uint32_t* ticket,
                        unsigned long long* out, uint32_t* err, cudaStream_t stream);
+// sums[c] = sum of chunk c = keys[c * chunk, min(n, (c + 1) * chunk)) and
+// *total (zeroed by the caller) += every chunk's sum, modulo 2^64.
+cudaError_t launch_sum_chunks(const void* keys, size_t n, int elem_kind, size_t chunk, unsigned long long* sums,
+                              unsigned long long* total, cudaStream_t stream);
 
 // ---- select (pa_select.cu) -------------------------------------------------
 struct SelectState;
@@ -185,5 +198,11 @@ size_t select_state_bytes();
 // launcher).
 cudaError_t launch_select(const void* keys, size_t n, size_t k, int key_bytes, void* cand, size_t cand_cap,
                           void* work, void* out, uint32_t* err, cudaStream_t stream);
+// *idx = k when keys[k] == *value, else the smallest index of a key equal to
+// *value in keys[0, n) (all ones if none).
+cudaError_t launch_find_key(const uint32_t* keys, size_t n, size_t k, const uint32_t* value, unsigned long long* idx,
+                            cudaStream_t stream);
+// Swaps keys[k] and keys[*idx] unless *idx is k or not below n.
+cudaError_t launch_swap_key(uint32_t* keys, size_t n, size_t k, const unsigned long long* idx, cudaStream_t stream);
 
 }  // namespace pa

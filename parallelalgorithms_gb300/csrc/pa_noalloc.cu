@@ -20,9 +20,10 @@
 // threads) would race on the array: issue them one after the other.
 //
 // Host code cannot use the array's name as a device address, so the first
-// call on each device looks the address up with cudaGetSymbolAddress (with
-// that device current) and caches it; make that first call before any
-// stream capture.
+// call on each device that needs the scratch looks the address up with
+// cudaGetSymbolAddress (with that device current) and caches it; make that
+// first call before any stream capture.  Up to 8192 keys the call sorts in
+// one CTA's shared memory, as pa_sort_u32 does, and touches no scratch.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -112,15 +113,26 @@ extern "C" int pa_sort_u32_noalloc(uint32_t* keys, uint32_t* tmp, size_t n, cons
     return fail(PA_ERR_ARG,
                 "pa_sort_u32_noalloc: keys and tmp must be device memory of the current device (host buffers "
                 "would need staging memory; use pa_sort_u32)");
+  cudaStream_t stream = opts ? static_cast<cudaStream_t>(opts->stream) : (cudaStream_t)0;
+  char why[200];
+  if (n <= small_sort_max_keys(4, false)) {
+    // Up to 8192 keys pa_sort_u32 sorts in one CTA's shared memory; that
+    // kernel needs no global scratch, so this call runs it as is.
+    cudaError_t e = launch_small_sort(keys, nullptr, n, 4, false, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) {
+      snprintf(why, sizeof(why), "pa_sort_u32_noalloc: %s", cudaGetErrorString(e));
+      return fail(PA_ERR_CUDA, why);
+    }
+    return PA_OK;
+  }
   const size_t tile = onesweep_tile_keys(4, false);
   const size_t tiles = (n + tile - 1) / tile;
   if ((size_t)kPasses * tiles * 256 * 4 > kStatusBytes)
     return fail(PA_ERR_ARG, "pa_sort_u32_noalloc: the selected tile geometry needs more look-back words than the scratch holds");
 
   unsigned char* base = nullptr;
-  char why[200];
   if (int rc = scratch_for_current_device(&base, why, sizeof(why))) return fail(rc, why);
-  cudaStream_t stream = opts ? static_cast<cudaStream_t>(opts->stream) : (cudaStream_t)0;
   auto* counts = reinterpret_cast<unsigned long long*>(base + kCountsOff);
   auto* tickets = reinterpret_cast<uint32_t*>(base + kTicketsOff);
   auto* err = reinterpret_cast<uint32_t*>(base + kErrOff);

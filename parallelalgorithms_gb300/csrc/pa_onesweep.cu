@@ -77,6 +77,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
   job.bin_start = args.bin_start;
   job.status = static_cast<S*>(args.status);
   job.err = args.err;
+  job.spin_limit = args.spin_limit ? args.spin_limit : kSpinLimit;
   uint32_t parity = 0;
   if constexpr (MULTISPLIT)
     onesweep_tile_multisplit<K, HAS_VALS, BLOCK, ITEMS, S>(job, smem, s_bar, parity);
@@ -205,7 +206,8 @@ cudaError_t launch_g2(const OnesweepArgs& a, cudaStream_t stream) {
   auto kern = onesweep_kernel<K, HAS_VALS, BLOCK, ITEMS, MINB, S, MS>;
   cudaError_t e = ensure_dynamic_smem(kern, G::kBytes);
   if (e != cudaSuccess) return e;
-  const size_t tiles = ceil_div(a.n, (size_t)G::kTile);
+  size_t tiles = ceil_div(a.n, (size_t)G::kTile);
+  if (a.max_ctas && a.max_ctas < tiles) tiles = a.max_ctas;
   kern<<<(unsigned)tiles, BLOCK, G::kBytes, stream>>>(a);
   return cudaGetLastError();
 }

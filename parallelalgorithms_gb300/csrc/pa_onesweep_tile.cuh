@@ -205,6 +205,7 @@ struct TileJob {
   const unsigned long long* bin_start;
   S* status;
   uint32_t* err;
+  uint32_t spin_limit;  // look-back polls before giving up (kSpinLimit unless a test lowers it)
 };
 
 // One tile of an onesweep digit pass (steps 2-6 above).  Called by all
@@ -268,8 +269,10 @@ __device__ __forceinline__ void onesweep_tile(const TileJob<K, S>& job, unsigned
     s_bin_start[i] = 0;
     s_bin_end[i] = 0;
   }
+  bool tma_pending = false;  // this thread's wait for the tile's bulk copy gave up
   if (tma_ok) {
-    if (!mbar_wait_bounded(s_bar, parity, job.err)) *s_abort = 1;
+    tma_pending = !mbar_wait_bounded(s_bar, parity, job.err);
+    if (tma_pending) *s_abort = 1;
     parity ^= 1u;
   }
   __syncthreads();
@@ -361,7 +364,7 @@ __device__ __forceinline__ void onesweep_tile(const TileJob<K, S>& job, unsigned
         t -= used;
         if (!done && used == 0) {
           ++spins;
-          if (spins > kSpinLimit || ((spins & 1023u) == 0 && ld_relaxed_gpu(job.err) != 0)) {
+          if (spins > job.spin_limit || ((spins & 1023u) == 0 && ld_relaxed_gpu(job.err) != 0)) {
             raise_error(job.err, DEVERR_LOOKBACK_TIMEOUT);
             *s_abort = 1;
             break;
@@ -378,7 +381,12 @@ __device__ __forceinline__ void onesweep_tile(const TileJob<K, S>& job, unsigned
   // ---- 6. write out in bin-contiguous runs -----------------------------------
   // A tile whose look-back or load gave up has no valid offsets: it writes
   // nothing (the call reports the failure), and every store is bounds-checked.
-  if (*s_abort) return;
+  // A bulk copy that was waited for in vain gets one more bounded wait, so
+  // that it cannot land in shared memory after the CTA has moved on.
+  if (*s_abort) {
+    if (tma_pending) mbar_wait_bounded(s_bar, parity ^ 1u, job.err);
+    return;
+  }
   const S n_out = (S)job.n;
   auto scatter = [&](auto transform) {
     if (full) {
@@ -554,8 +562,10 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
     for (uint32_t i = tid; i < tile_n; i += BLOCK) s_vals[i] = vin[tile_base + i];
   }
   for (uint32_t i = loaded + tid; i < tile_n; i += BLOCK) s_keys[i] = in[tile_base + i];
+  bool tma_pending = false;  // this thread's wait for the tile's bulk copy gave up
   if (tma_ok) {
-    if (!mbar_wait_bounded(s_bar, parity, job.err)) *s_abort = 1;
+    tma_pending = !mbar_wait_bounded(s_bar, parity, job.err);
+    if (tma_pending) *s_abort = 1;
     parity ^= 1u;
   }
   __syncthreads();
@@ -700,7 +710,7 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
           ++spins;
           // give up once the limit is reached, or early once another tile
           // has already reported a failure (its successors would wait in vain)
-          if (spins > kSpinLimit || ((spins & 1023u) == 0 && ld_relaxed_gpu(job.err) != 0)) {
+          if (spins > job.spin_limit || ((spins & 1023u) == 0 && ld_relaxed_gpu(job.err) != 0)) {
             raise_error(job.err, DEVERR_LOOKBACK_TIMEOUT);
             *s_abort = 1;
             break;
@@ -714,8 +724,12 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
   }
   __syncthreads();
 
-  // write out in bin-contiguous runs
-  if (*s_abort) return;
+  // write out in bin-contiguous runs (nothing after a failed wait; a bulk
+  // copy waited for in vain gets one more bounded wait first)
+  if (*s_abort) {
+    if (tma_pending) mbar_wait_bounded(s_bar, parity ^ 1u, job.err);
+    return;
+  }
   const S n_out = (S)job.n;
   auto scatter = [&](auto transform) {
     if (full) {

@@ -104,6 +104,7 @@ __device__ __forceinline__ void pass_item(const PlanDev& P, const Item& it, unsi
   job.bin_start = P.bin_start + (size_t)it.seg * 1024 + it.pass * 256;
   job.status = P.status + ((size_t)it.pass * P.total_tiles + L.tile_base) * 256;
   job.err = P.err;
+  job.spin_limit = kSpinLimit;
   onesweep_tile_multisplit<uint32_t, false, kBlock, PASS_ITEMS, uint32_t>(job, smem, bar, parity);
 }
 

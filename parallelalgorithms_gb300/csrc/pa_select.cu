@@ -650,9 +650,63 @@ __global__ void select_init_kernel(SelectState* st, unsigned long long k) {
   }
 }
 
+// Index of a key equal to *value in keys[0, n), into *idx (set to all ones
+// by the launcher first): k itself when keys[k] already holds it, else the smallest
+// such index.  CTAs walk 16 K-key chunks in chunk order; a chunk that starts
+// past an index already found is skipped, so the walk stops early.
+constexpr int kFindBlock = 256;
+constexpr size_t kFindChunk = (size_t)kFindBlock * 64;
+
+__global__ void __launch_bounds__(kFindBlock) find_key_kernel(const uint32_t* __restrict__ keys, size_t n, size_t k,
+                                                              const uint32_t* __restrict__ value,
+                                                              unsigned long long* idx) {
+  const uint32_t v = *value;
+  if (keys[k] == v) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicMin(idx, (unsigned long long)k);
+    return;
+  }
+  __shared__ unsigned long long s_best;
+  for (size_t c = blockIdx.x; c * kFindChunk < n; c += gridDim.x) {
+    const size_t lo = c * kFindChunk;
+    if (threadIdx.x == 0) s_best = ld_relaxed_gpu(idx);
+    __syncthreads();
+    const bool past = lo > s_best;
+    __syncthreads();
+    if (past) return;  // every later chunk starts later still
+    const size_t hi = min(n, lo + kFindChunk);
+    for (size_t i = lo + threadIdx.x; i < hi; i += kFindBlock)
+      if (keys[i] == v) atomicMin(idx, (unsigned long long)i);
+  }
+}
+
+// keys[k] <-> keys[*idx] (one thread); nothing when *idx is k or not found.
+__global__ void swap_key_kernel(uint32_t* keys, size_t n, size_t k, const unsigned long long* idx) {
+  const unsigned long long j = *idx;
+  if (j >= n || j == k) return;
+  const uint32_t t = keys[k];
+  keys[k] = keys[j];
+  keys[j] = t;
+}
+
 }  // namespace
 
 size_t select_state_bytes() { return sizeof(SelectState); }
+
+cudaError_t launch_find_key(const uint32_t* keys, size_t n, size_t k, const uint32_t* value, unsigned long long* idx,
+                            cudaStream_t stream) {
+  if (n == 0 || k >= n) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(idx, 0xFF, sizeof(*idx), stream);  // "not found yet"
+  if (e != cudaSuccess) return e;
+  const size_t chunks = ceil_div(n, kFindChunk);
+  const unsigned grid = (unsigned)min(chunks, (size_t)device_info().sm_count * 8);
+  find_key_kernel<<<grid, kFindBlock, 0, stream>>>(keys, n, k, value, idx);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_swap_key(uint32_t* keys, size_t n, size_t k, const unsigned long long* idx, cudaStream_t stream) {
+  swap_key_kernel<<<1, 1, 0, stream>>>(keys, n, k, idx);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_select(const void* keys, size_t n, size_t k, int key_bytes, void* cand, size_t cand_cap,
                           void* work, void* out, uint32_t* err, cudaStream_t stream) {

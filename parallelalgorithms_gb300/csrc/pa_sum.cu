@@ -6,7 +6,11 @@
 // with shuffles,
 // each CTA writes one partial, and the last CTA to finish (ticket) adds the
 // partials in CTA order.  Integer addition modulo 2^64 is associative, so
-// the result equals the reference's bit for bit whatever the split.
+// the result equals the reference's bit for bit whatever the split.  Any
+// element type of 1, 2, 4 or 8 bytes is summed the same way after widening
+// to 64 bits (the reference's template SumParallel<_Type>, :207-237).
+#include <type_traits>
+
 #include "pa_bulkstream.cuh"
 #include "pa_common.cuh"
 #include "pa_kernels.cuh"
@@ -23,6 +27,44 @@ constexpr int kConsumers = 512;
 using Ring = BulkRing<kStages, kChunk, kConsumers>;
 constexpr int kMaxSumBlocks = 152 * 8;
 
+// Element kinds (pa_gpu.h PA_ELEM_*): each element is widened to 64 bits
+// (zero-extended unsigned, sign-extended signed, float and double truncated
+// toward zero as the reference's (long long) cast does; out-of-range values,
+// undefined behaviour in the reference, saturate here) and summed modulo 2^64.
+template <typename T>
+__device__ __forceinline__ unsigned long long widen(T x) {
+  if constexpr (std::is_floating_point<T>::value || std::is_signed<T>::value)
+    return (unsigned long long)(long long)x;
+  else
+    return (unsigned long long)x;
+}
+
+// Sum of the elements of one 16-byte vector.
+template <typename T>
+__device__ __forceinline__ unsigned long long vec_sum(const uint4& a) {
+  if constexpr (std::is_same<T, uint32_t>::value) {
+    return (unsigned long long)a.x + a.y + (unsigned long long)a.z + a.w;
+  } else if constexpr (std::is_same<T, unsigned long long>::value) {
+    return ((unsigned long long)a.y << 32 | a.x) + ((unsigned long long)a.w << 32 | a.z);
+  } else if constexpr (std::is_same<T, uint8_t>::value || std::is_same<T, int8_t>::value) {
+    // byte sums of each word by sum-of-absolute-differences against zero
+    const uint32_t u = __vsadu4(a.x, 0u) + __vsadu4(a.y, 0u) + __vsadu4(a.z, 0u) + __vsadu4(a.w, 0u);
+    if constexpr (std::is_same<T, uint8_t>::value) {
+      return u;
+    } else {  // a signed byte b >= 128 stands for b - 256
+      const uint32_t neg = __popc(a.x & 0x80808080u) + __popc(a.y & 0x80808080u) + __popc(a.z & 0x80808080u) +
+                           __popc(a.w & 0x80808080u);
+      return (unsigned long long)((long long)u - 256ll * (long long)neg);
+    }
+  } else {
+    const T* e = reinterpret_cast<const T*>(&a);
+    unsigned long long acc = 0;
+#pragma unroll
+    for (int i = 0; i < (int)(16 / sizeof(T)); ++i) acc += widen(e[i]);
+    return acc;
+  }
+}
+
 template <typename K>
 __global__ void __launch_bounds__(Ring::kThreads, 1) sum_kernel(const K* __restrict__ keys, size_t n,
                                                                unsigned long long* __restrict__ partials,
@@ -38,18 +80,12 @@ __global__ void __launch_bounds__(Ring::kThreads, 1) sum_kernel(const K* __restr
 
   unsigned long long acc = 0;
   bulk_stream<kStages, kChunk, kConsumers>(keys + head, nvec * 16, ring, err, [&](const uint4* st, uint32_t nv) {
-    for (uint32_t v = threadIdx.x; v < nv; v += kConsumers) {
-      const uint4 a = st[v];
-      if (sizeof(K) == 4)
-        acc += (unsigned long long)a.x + a.y + (unsigned long long)a.z + a.w;
-      else
-        acc += ((unsigned long long)a.y << 32 | a.x) + ((unsigned long long)a.w << 32 | a.z);
-    }
+    for (uint32_t v = threadIdx.x; v < nv; v += kConsumers) acc += vec_sum<K>(st[v]);
   });
   if (blockIdx.x == 0) {
     const size_t rest = head + (n - tail_start);
     for (size_t r = threadIdx.x; r < rest; r += Ring::kThreads)
-      acc += (unsigned long long)keys[r < head ? r : tail_start + (r - head)];
+      acc += widen(keys[r < head ? r : tail_start + (r - head)]);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
@@ -91,17 +127,88 @@ cudaError_t launch_sum_t(const K* keys, size_t n, unsigned long long* partials, 
   return cudaGetLastError();
 }
 
+// Per-chunk sums: chunk c is keys[c * chunk, min(n, (c + 1) * chunk)).  One
+// warp per chunk (warps stride over chunks); lanes read the chunk coalesced,
+// lane 0 stores its sum and adds it to *total (addition modulo 2^64 is
+// associative, so the atomic order does not matter).
+template <typename K>
+__global__ void __launch_bounds__(256) sum_chunks_kernel(const K* __restrict__ keys, size_t n, size_t chunk,
+                                                         size_t nchunks, unsigned long long* __restrict__ sums,
+                                                         unsigned long long* total) {
+  const size_t warps = (size_t)gridDim.x * (blockDim.x / 32);
+  const uint32_t lane = threadIdx.x & 31u;
+  for (size_t c = (size_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); c < nchunks; c += warps) {
+    const size_t lo = c * chunk, hi = min(n, lo + chunk);
+    unsigned long long acc = 0;
+    for (size_t i = lo + lane; i < hi; i += 32) acc += widen(keys[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+    if (lane == 0) {
+      sums[c] = acc;
+      atomicAdd(total, acc);
+    }
+  }
+}
+
+template <typename K>
+cudaError_t launch_chunks_t(const void* keys, size_t n, size_t chunk, unsigned long long* sums,
+                            unsigned long long* total, cudaStream_t stream) {
+  const size_t nchunks = ceil_div(n, chunk);
+  const size_t grid = min(ceil_div(nchunks, (size_t)8), (size_t)device_info().sm_count * 16);
+  sum_chunks_kernel<K><<<(unsigned)(grid < 1 ? 1 : grid), 256, 0, stream>>>(static_cast<const K*>(keys), n, chunk,
+                                                                           nchunks, sums, total);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 size_t sum_partials_needed() { return kMaxSumBlocks; }
 
-cudaError_t launch_sum(const void* keys, size_t n, int key_bytes, unsigned long long* partials, uint32_t* ticket,
+int sum_elem_bytes(int elem_kind) {
+  switch (elem_kind) {
+    case kElemU8: case kElemI8: return 1;
+    case kElemU16: case kElemI16: return 2;
+    case kElemU32: case kElemI32: case kElemF32: return 4;
+    case kElemU64: case kElemI64: case kElemF64: return 8;
+    default: return 0;
+  }
+}
+
+cudaError_t launch_sum(const void* keys, size_t n, int elem_kind, unsigned long long* partials, uint32_t* ticket,
                        unsigned long long* out, uint32_t* err, cudaStream_t stream) {
-  if (key_bytes == 4)
-    return launch_sum_t(static_cast<const uint32_t*>(keys), n, partials, ticket, out, err, stream);
-  if (key_bytes == 8)
-    return launch_sum_t(static_cast<const unsigned long long*>(keys), n, partials, ticket, out, err, stream);
-  return cudaErrorInvalidValue;
+  switch (elem_kind) {
+    case kElemU8: return launch_sum_t(static_cast<const uint8_t*>(keys), n, partials, ticket, out, err, stream);
+    case kElemI8: return launch_sum_t(static_cast<const int8_t*>(keys), n, partials, ticket, out, err, stream);
+    case kElemU16: return launch_sum_t(static_cast<const uint16_t*>(keys), n, partials, ticket, out, err, stream);
+    case kElemI16: return launch_sum_t(static_cast<const int16_t*>(keys), n, partials, ticket, out, err, stream);
+    case kElemU32: return launch_sum_t(static_cast<const uint32_t*>(keys), n, partials, ticket, out, err, stream);
+    case kElemI32: return launch_sum_t(static_cast<const int32_t*>(keys), n, partials, ticket, out, err, stream);
+    case kElemU64:
+      return launch_sum_t(static_cast<const unsigned long long*>(keys), n, partials, ticket, out, err, stream);
+    case kElemI64: return launch_sum_t(static_cast<const long long*>(keys), n, partials, ticket, out, err, stream);
+    case kElemF32: return launch_sum_t(static_cast<const float*>(keys), n, partials, ticket, out, err, stream);
+    case kElemF64: return launch_sum_t(static_cast<const double*>(keys), n, partials, ticket, out, err, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_sum_chunks(const void* keys, size_t n, int elem_kind, size_t chunk, unsigned long long* sums,
+                              unsigned long long* total, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  if (chunk == 0) return cudaErrorInvalidValue;
+  switch (elem_kind) {
+    case kElemU8: return launch_chunks_t<uint8_t>(keys, n, chunk, sums, total, stream);
+    case kElemI8: return launch_chunks_t<int8_t>(keys, n, chunk, sums, total, stream);
+    case kElemU16: return launch_chunks_t<uint16_t>(keys, n, chunk, sums, total, stream);
+    case kElemI16: return launch_chunks_t<int16_t>(keys, n, chunk, sums, total, stream);
+    case kElemU32: return launch_chunks_t<uint32_t>(keys, n, chunk, sums, total, stream);
+    case kElemI32: return launch_chunks_t<int32_t>(keys, n, chunk, sums, total, stream);
+    case kElemU64: return launch_chunks_t<unsigned long long>(keys, n, chunk, sums, total, stream);
+    case kElemI64: return launch_chunks_t<long long>(keys, n, chunk, sums, total, stream);
+    case kElemF32: return launch_chunks_t<float>(keys, n, chunk, sums, total, stream);
+    case kElemF64: return launch_chunks_t<double>(keys, n, chunk, sums, total, stream);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace pa

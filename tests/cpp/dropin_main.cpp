@@ -42,6 +42,14 @@ int main(int argc, char** argv) {
   std::vector<unsigned> a3(uints), b3(n);
   ParallelAlgorithms::RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase(a3.data(), b3.data(), n);
   if (a3 != ref || b3 != ref) return fail("RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase");
+  std::vector<unsigned> a4(uints), b4(n);
+  ParallelAlgorithms::RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase_DeRandomize(a4.data(), b4.data(), n);
+  if (b4 != ref) return fail("RadixSortLSDPowerOf2RadixParallel_unsigned_TwoPhase_DeRandomize");
+  std::vector<unsigned> a5(uints), w5(n);
+  ParallelAlgorithms::SortRadixInnerPar<256, 8>(a5.data(), w5.data(), n);
+  if (a5 != ref) return fail("SortRadixInnerPar<256,8>");
+  ParallelAlgorithms::SortRadixInnerPar<256, 8>(a5.data(), w5.data(), n, n / 8);  // explicit quantum
+  if (a5 != ref) return fail("SortRadixInnerPar<256,8>(quantum)");
 
   // HistogramByteComponentsParallel<256,8>: 8 rows, rows 4-7 zero
   size_t** h = ParallelAlgorithms::HistogramByteComponentsParallel<256, 8>(uints.data(), 0, n - 1);
@@ -70,12 +78,55 @@ int main(int argc, char** argv) {
     std::nth_element(nth.begin(), nth.begin() + k, nth.end());
     unsigned v = SelectRadix(s.data(), n, k);
     if (v != nth[k] || s[k] != nth[k]) return fail("SelectRadix");
+    std::vector<unsigned> s_sorted(s);
+    std::sort(s_sorted.begin(), s_sorted.end());
+    if (s_sorted != ref) return fail("SelectRadix left a permutation of the input");
   }
 
   // SumParallelNonRecursive vs std::accumulate
   const unsigned long long sref = std::accumulate(uints.begin(), uints.end(), 0ULL);
   if (ParallelAlgorithms::SumParallelNonRecursive(uints.data(), 0, n) != sref) return fail("SumParallelNonRecursive");
   if ((unsigned long long)ParallelAlgorithms::SumParallel(uints.data(), 0, n) != sref) return fail("SumParallel");
+  if (ParallelAlgorithms::SumParallelNonRecursiveBufferedLocally(uints.data(), 0, n) != sref ||
+      ParallelAlgorithms::SumParallelNonRecursiveBuffered(uints.data(), 0, n) != sref)
+    return fail("SumParallelNonRecursiveBuffered(Locally)");
+  {
+    // the caller-buffer form: each parallelThreshold chunk's sum lands in sum_array
+    const size_t thr = 16 * 1024, tasks = (n + thr - 1) / thr;
+    std::vector<unsigned long long> sum_array(tasks, 0);
+    if (ParallelAlgorithms::SumParallelNonRecursive(uints.data(), 0, n, sum_array.data(), thr) != sref)
+      return fail("SumParallelNonRecursive(sum_array)");
+    for (size_t t = 0; t < tasks; ++t) {
+      const size_t hi = std::min(n, (t + 1) * thr);
+      if (sum_array[t] != std::accumulate(uints.begin() + t * thr, uints.begin() + hi, 0ULL))
+        return fail("SumParallelNonRecursive(sum_array) chunk");
+    }
+    std::vector<unsigned long long> u64(uints.begin(), uints.end());
+    if (ParallelAlgorithms::SumParallel(u64.data(), 0, n) != sref ||
+        ParallelAlgorithms::SumParallelNonRecursive(u64.data(), 0, n) != sref)
+      return fail("SumParallel(u64)");
+  }
+  {
+    // SumBenchmarkChar's call (SumBenchmark.cpp:72-110): the template
+    // SumParallel over unsigned chars, against a plain 64-bit accumulation
+    std::vector<unsigned char> u8Array(n);
+    for (size_t i = 0; i < n; ++i) u8Array[i] = (unsigned char)uints[i];
+    long long sum_ref = 0;
+    for (unsigned char c : u8Array) sum_ref += (long long)c;
+    long long sum = ParallelAlgorithms::SumParallel(u8Array.data(), 0, uints.size());
+    if (sum != sum_ref) return fail("SumParallel(unsigned char)");
+    std::vector<int> i32(n);
+    std::vector<float> f32(n);
+    long long i_ref = 0, f_ref = 0;
+    for (size_t i = 0; i < n; ++i) {
+      i32[i] = (int)uints[i];
+      f32[i] = (float)(int)(uints[i] >> 8) / 7.0f - 100000.0f;
+      i_ref += (long long)i32[i];
+      f_ref += (long long)f32[i];
+    }
+    if (ParallelAlgorithms::SumParallel(i32.data(), 0, n) != i_ref) return fail("SumParallel(int)");
+    if (ParallelAlgorithms::SumParallel(f32.data(), 0, n) != f_ref) return fail("SumParallel(float)");
+  }
 
   // counting_sort_parallel vs std::sort of the same bytes
   {

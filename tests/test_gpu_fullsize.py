@@ -1,8 +1,12 @@
 """The 100M-key workloads (uniform, presorted 0..n-1, constant 42; 64-bit
 keys with payload; float32 with specials) on the GPU, checked bit-exact
-against the oracle restatement (C, a few seconds per sort at this size) and
-through size-independent properties: sortedness, histogram and sum
-invariance under the permutation, stability of the index payload."""
+against the reference's own code compiled unchanged (SortRadixPar,
+HistogramOneByteComponentParallel, HistogramByteComponentsParallel,
+SelectRadix and SumParallelNonRecursive on this host's cores, tens of ms
+each at this size), against the oracle restatement, against numpy's stable
+argsort for the key + index payload case, and through size-independent
+properties: sortedness, histogram and sum invariance under the permutation,
+stability of the index payload."""
 import numpy as np
 import pytest
 
@@ -37,6 +41,30 @@ def test_u32_100m_sort_histogram_select_sum(pa, port, torch_cuda, inputs, dist):
         assert pa.select(a, k) == int(want[k])
 
 
+@pytest.mark.parametrize("dist", ["uniform", "presorted", "constant"])
+def test_u32_100m_against_the_compiled_reference(pa, ref, torch_cuda, inputs, dist):
+    """The C2 calls on each 100M array, the GPU against the reference's own
+    code (RadixSortLsdBenchmark.cpp:95-110, RadixSelectBenchmark.cpp:51-66,
+    SumBenchmark.cpp:135-160 make the same calls)."""
+    a = inputs[dist]
+    want = ref.sort_radix_par(a.copy())
+    d = torch_cuda.from_numpy(a.view(np.int32)).cuda()
+    pa.SortRadixPar(d, torch_cuda.empty_like(d), N)
+    np.testing.assert_array_equal(d.cpu().numpy().view(np.uint32), want)
+    del d
+    np.testing.assert_array_equal(pa.HistogramOneByteComponentParallel(a, 0, N - 1, 0),
+                                  ref.hist_one_byte(a, 0, N - 1, 0))
+    np.testing.assert_array_equal(pa.HistogramByteComponentsParallel(a, 0, N - 1),
+                                  ref.hist_byte_components(a, 0, N - 1))
+    for k in (N // 2, N - 21):
+        v = ref.select(a, k)
+        assert v == int(want[k])
+        c = a.copy()
+        assert pa.SelectRadix(c, N, k) == v
+        assert c[k] == v
+    assert pa.SumParallelNonRecursive(a, 0, N) == ref.sum_nonrec(a)
+
+
 def test_u64_kv_100m_stable(pa, port):
     from parallelalgorithms_gb300 import workloads
     for keys in (workloads.uniform_u64(N), workloads.zipf_u64(N)):
@@ -50,6 +78,8 @@ def test_u64_kv_100m_stable(pa, port):
         wk, wv = port.sort(keys, vals)
         np.testing.assert_array_equal(k, wk)
         np.testing.assert_array_equal(v, wv)
+        # independent of the restatement: numpy's stable argsort gives the payload
+        np.testing.assert_array_equal(v, np.argsort(keys, kind="stable").astype(np.uint32))
 
 
 def test_f32_100m_total_order(pa, port):

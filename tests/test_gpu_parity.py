@@ -167,11 +167,37 @@ def test_select_matches_oracle(pa, port, n):
             c = a.copy()
             assert pa.SelectRadix(c, n, k) == want
             assert c[k] == want  # the reference leaves the k-th element at a[k]
+            # only a[k] and the first element holding the answer may trade places
+            np.testing.assert_array_equal(np.sort(c), np.sort(a))
+            assert np.count_nonzero(c != a) in (0, 2)
     if n > 100:
         a = u32_inputs(n)["uniform"]
         start, length = 17, n - 40
         k = start + length // 3
-        assert pa.SelectRadix(a.copy(), start, length, k) == port.select(a, k, start=start, length=length)
+        c = a.copy()
+        assert pa.SelectRadix(c, start, length, k) == port.select(a, k, start=start, length=length)
+        np.testing.assert_array_equal(np.sort(c), np.sort(a))
+        np.testing.assert_array_equal(c[:start], a[:start])
+        np.testing.assert_array_equal(c[start + length:], a[start + length:])
+
+
+@pytest.mark.parametrize("n", [1, 1000, 1 << 20])
+def test_select_radix_device_array_stays_a_permutation(pa, port, torch_cuda, n):
+    """SelectRadix on a device array: a[k] holds the answer, a[k] and the
+    first element holding the answer traded places, nothing else moved."""
+    for name, a in u32_inputs(n).items():
+        k = n // 3
+        want = port.select(a, k)
+        d = torch_cuda.from_numpy(a.view(np.int32).copy()).cuda()
+        assert pa.SelectRadix(d, n, k) == want
+        c = d.cpu().numpy().view(np.uint32)
+        assert c[k] == want, name
+        diff = np.flatnonzero(c != a)
+        assert diff.size in (0, 2), name
+        if diff.size:
+            j = diff[diff != k][0]
+            assert a[j] == want and c[j] == a[k]
+            assert not np.any(a[:j] == want)  # the first place that held it
 
 
 def test_select_sample_bracket_paths(pa, port):
@@ -373,3 +399,61 @@ def test_radix_leaf_merge_sorts(pa, ref, torch_cuda, n):
         got = dd.cpu().numpy().view(np.uint32)
         np.testing.assert_array_equal(got[l:r + 1], np.sort(a[l:r + 1]))
         assert not got[:l].any() and not got[r + 1:].any()
+
+
+TYPED = [np.uint8, np.int8, np.uint16, np.int16, np.uint32, np.int32, np.uint64, np.int64, np.float32, np.float64]
+
+
+def _typed_input(dtype, n, seed):
+    rng = np.random.default_rng(seed)
+    if np.issubdtype(dtype, np.floating):
+        a = (rng.standard_normal(n) * 1e6).astype(dtype)
+        if n > 10:
+            a[3], a[7] = dtype(-0.0), dtype(2.5e9)
+        return a
+    info = np.iinfo(dtype)
+    return rng.integers(info.min, info.max, n, dtype=dtype, endpoint=True)
+
+
+def _template_sum(a) -> int:
+    """template SumParallel<_Type> (SumParallel.h:207-237): each element cast
+    to long long (floats truncated toward zero), summed modulo 2^64, read as
+    signed; the unsigned long long overload (:162) returns the unsigned sum."""
+    if a.dtype == np.uint64:
+        return int(np.sum(a, dtype=np.uint64))
+    w = np.trunc(a).astype(np.int64) if np.issubdtype(a.dtype, np.floating) else a.astype(np.int64)
+    return int(np.sum(w, dtype=np.int64))
+
+
+@pytest.mark.parametrize("dtype", TYPED)
+@pytest.mark.parametrize("n", [0, 1, 17, 4097, 1_000_003])
+def test_typed_sum_is_the_template_sum(pa, dtype, n):
+    a = _typed_input(dtype, n, n + 7)
+    assert pa.SumParallel(a, 0, n) == _template_sum(a)
+    if n > 10:
+        assert pa.SumParallel(a, 3, n - 2) == _template_sum(a[3:n - 2])  # unaligned start
+
+
+def test_typed_sum_against_the_compiled_reference(pa, ref):
+    for dtype in (np.uint8, np.uint32, np.int32, np.float32):
+        for n in (1, 1000, 1_000_003):
+            a = _typed_input(dtype, n, n)
+            assert pa.SumParallel(a, 0, n) == ref.sum_template(a), (dtype, n)
+
+
+@pytest.mark.parametrize("n,threshold", [(1, 16384), (100_000, 16384), (1_000_003, 1000), (65536, 16384),
+                                         (5, 1)])
+def test_chunked_sums_fill_the_callers_sum_array(pa, ref, n, threshold):
+    a = workloads_u32(n)
+    l, r = (2, n - 1) if n > 4 else (0, n)
+    tasks = -(-(r - l) // threshold)
+    arr = np.zeros(tasks, np.uint64)
+    total = pa.SumParallelNonRecursive(a, l, r, arr, threshold)
+    want_total, want_arr = ref.sum_nonrec_array(a, l, r, threshold)
+    assert total == want_total
+    np.testing.assert_array_equal(arr, want_arr)
+
+
+def workloads_u32(n):
+    from parallelalgorithms_gb300 import workloads
+    return workloads.uniform_u32(n)

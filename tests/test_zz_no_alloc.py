@@ -1,10 +1,11 @@
 """pa_sort_u32_noalloc, the sort entry point for callers that cannot
 allocate GPU memory (a framework's caching allocator owns all of it, or a
 cudaMalloc's device-wide synchronisation is not acceptable), checked
-through the C ABI against pa_sort_u32 on the same inputs.
+through the C ABI against pa_sort_u32 and the oracle restatement on the
+same inputs.
 
-Kept in a file of its own that pytest collects last.  Two calls in a row
-show that a call is unaffected by what the previous call left in the shared
+Kept in a file of its own that pytest collects last.  Calls in a row show
+that a call is unaffected by what the previous call left in the shared
 scratch array."""
 import ctypes
 
@@ -29,7 +30,7 @@ def _sort_both(lib, torch, a: np.ndarray):
     return got.cpu().numpy().view(np.uint32), want.cpu().numpy().view(np.uint32)
 
 
-def test_noalloc_sort_matches_pa_sort_u32_two_calls_in_a_row(pa, torch_cuda):
+def test_noalloc_sort_matches_pa_sort_u32_two_calls_in_a_row(pa, port, torch_cuda):
     from parallelalgorithms_gb300 import workloads
     lib = pa.lib()
     first = workloads.uniform_u32(MAX_KEYS)                                   # the largest size allowed
@@ -37,7 +38,19 @@ def test_noalloc_sort_matches_pa_sort_u32_two_calls_in_a_row(pa, torch_cuda):
     for a in (first, second):
         got, want = _sort_both(lib, torch_cuda, a)
         np.testing.assert_array_equal(got, want)
-        assert np.all(got[1:] >= got[:-1])
+        np.testing.assert_array_equal(got, port.sort(a)[0])
+
+
+@pytest.mark.parametrize("n", [1, 2, 6143, 6144, 8192, 8193, 12289])
+def test_noalloc_sort_small_and_one_tile_sizes(pa, port, torch_cuda, n):
+    """Sizes around the one-CTA shared-memory sort's limit (8192 keys) and the
+    onesweep tile (6144 keys): the same result as pa_sort_u32 and the oracle."""
+    lib = pa.lib()
+    for seed in (n, n + 1):  # two calls in a row
+        a = np.random.default_rng(seed).integers(0, 2**32, n, dtype=np.uint32)
+        got, want = _sort_both(lib, torch_cuda, a)
+        np.testing.assert_array_equal(got, want)
+        np.testing.assert_array_equal(got, port.sort(a)[0])
 
 
 def test_noalloc_sort_rejects_what_it_cannot_do_without_allocating(pa, torch_cuda):
