@@ -514,8 +514,9 @@ __device__ __forceinline__ void order_tile_in_place(K* s_keys, uint32_t tile_n) 
 // j * 32 + l; for each item the lanes holding the same digit (its peers) are
 // found with the eight ballots of match_digit8, or for every PA_MATCH_MIX-th
 // item by an atomic OR of the lane bit into the warp's shared word for the
-// digit; one lane of the group bumps the warp's counter for that digit and
-// every lane takes counter + peers below it, so ranks follow tile order.
+// digit; every lane reads the warp's counter for that digit and takes
+// counter + peers below it, then the group's lowest lane bumps the counter,
+// so ranks follow tile order.
 // Per-bin warp counters are scanned across warps into tile offsets; keys are
 // staged in shared memory at their in-tile sorted position and written out
 // in bin-contiguous runs after the look-back.
@@ -562,6 +563,11 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
     for (uint32_t i = tid; i < tile_n; i += BLOCK) s_vals[i] = vin[tile_base + i];
   }
   for (uint32_t i = loaded + tid; i < tile_n; i += BLOCK) s_keys[i] = in[tile_base + i];
+  // A short last tile is padded with all-ones keys: they rank after every
+  // real key (in bin 255, after its real keys), so every tile is ranked as a
+  // full one; they only raise the last tile's own bin-255 count, which no
+  // later tile reads, and they are never written out.
+  for (uint32_t i = tile_n + tid; i < (uint32_t)TILE; i += BLOCK) s_keys[i] = ~(K)0;
   bool tma_pending = false;  // this thread's wait for the tile's bulk copy gave up
   if (tma_ok) {
     tma_pending = !mbar_wait_bounded(s_bar, parity, job.err);
@@ -588,42 +594,33 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
   auto rank_item = [&](auto jc) {
     constexpr int j = decltype(jc)::value;
     const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
-    const bool valid = full || idx < tile_n;
-    k[j] = valid ? s_keys[idx] : (K)0;
-    if (HAS_VALS) v[j] = valid ? s_vals[idx] : 0u;
+    k[j] = s_keys[idx];
+    if (HAS_VALS) v[j] = s_vals[idx];
     const uint32_t d = digit8(k[j], dsel, dupper);
 #if PA_MATCH_ATOMIC_OR || PA_MATCH_MIX
     constexpr bool kSmemMatch = PA_MATCH_ATOMIC_OR || (PA_MATCH_MIX > 0 && j % (PA_MATCH_MIX > 0 ? PA_MATCH_MIX : 1) == 0);
 #else
     constexpr bool kSmemMatch = false;
 #endif
-    uint32_t peers, leader, base = 0;
+    uint32_t peers;
+    uint32_t* mw = s_wh + WARPS * kRadix + warp * kRadix + d;
     if constexpr (kSmemMatch) {
-      uint32_t* mw = s_wh + WARPS * kRadix + warp * kRadix + d;
-      if (valid) atomicOr(mw, 1u << lane);
+      atomicOr(mw, 1u << lane);
       __syncwarp();
-      peers = valid ? *mw : 0u;
-      __syncwarp();
-      leader = 31u - __clz(peers | (valid ? 0u : 1u));
-      if (lane == leader && valid) {
-        base = wh[d];
-        wh[d] = base + __popc(peers);
-        *mw = 0u;
-      }
+      peers = *mw;
     } else {
       peers = match_digit8(d);
-      if (!full) {
-        const uint32_t vm = __ballot_sync(FULL, valid);
-        peers &= valid ? vm : ~vm;
-      }
-      leader = __ffs(peers) - 1;
-      if (lane == leader && valid) {
-        base = wh[d];
-        wh[d] = base + __popc(peers);
-      }
     }
-    base = __shfl_sync(FULL, base, leader);
-    rk[j / 2] |= (base + __popc(peers & lt)) << (16 * (j % 2));
+    // Every lane reads the warp's counter for its digit; after the warp has
+    // read, the group's lowest lane bumps it (and clears the match word).
+    const uint32_t pl = peers & lt;
+    const uint32_t base = wh[d];
+    __syncwarp();
+    if (pl == 0) {
+      wh[d] = base + __popc(peers);
+      if constexpr (kSmemMatch) *mw = 0u;
+    }
+    rk[j / 2] |= (base + __popc(pl)) << (16 * (j % 2));
     __syncwarp();
   };
   static_for<ITEMS>(rank_item);
@@ -675,12 +672,9 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
   // stage keys at their in-tile sorted position; then the look-back
 #pragma unroll
   for (int j = 0; j < ITEMS; ++j) {
-    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
-    if (full || idx < tile_n) {
-      const uint32_t pos = wh[digit8(k[j], dsel, dupper)] + ((rk[j / 2] >> (16 * (j % 2))) & 0xFFFFu);
-      s_keys[pos] = k[j];
-      if (HAS_VALS) s_vals[pos] = v[j];
-    }
+    const uint32_t pos = wh[digit8(k[j], dsel, dupper)] + ((rk[j / 2] >> (16 * (j % 2))) & 0xFFFFu);
+    s_keys[pos] = k[j];
+    if (HAS_VALS) s_vals[pos] = v[j];
   }
   if (tid < (uint32_t)kRadix) {
     const uint32_t count = s_tcount[tid];
