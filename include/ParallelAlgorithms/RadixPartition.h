@@ -3,8 +3,9 @@
 // around one or several ascending indices k.  Afterwards each listed a[k] is
 // the k-th smallest of the range, nothing before it is larger and nothing
 // after it is smaller; the order inside each part differs from the
-// reference's swap loop (the GPU sorts the range, which partitions it around
-// every k at once).
+// reference's swap loop (for a few k the GPU selects each k-th smallest and
+// splits the keys into the buckets between them; for many k it sorts the
+// range, which partitions it around every k at once).
 #ifndef PA_DROPIN_RADIXPARTITION_H
 #define PA_DROPIN_RADIXPARTITION_H
 

@@ -302,8 +302,10 @@ int pa_sort_copy_u32(uint32_t* src, uint32_t* dst, size_t n, const pa_opts* opts
  * k[i], a[k[i]] is the k[i]-th smallest key, no key before it is larger and
  * no key after it is smaller -- the reference's contract.  The order of the
  * other keys inside each part differs from the reference's (an artefact of
- * its serial in-place swap loop): here the whole array comes out sorted, the
- * GPU's cheapest way to partition around many k at once. */
+ * its serial in-place swap loop): with at most 6 k the keys are split into
+ * the buckets the k-th smallest values define (one select per k, then one
+ * bucket pass; order inside a bucket unspecified), with more k the whole
+ * array comes out sorted (one sort partitions around every k at once). */
 int pa_partition_radix_u32(uint32_t* a, size_t n, const size_t* k, size_t k_len, const pa_opts* opts);
 
 /* Failure-detection self-test (no reference counterpart; the reference has

@@ -72,6 +72,11 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 constexpr int kMaxEvents = 16;
 
+// PartitionRadix with at most this many k runs one select per k and one
+// bucket pass; with more it sorts (a select costs about a sixth of a sort).
+constexpr size_t kPartitionSelectMax = 6;
+static_assert(kPartitionSelectMax <= (size_t)kPartitionMaxPivots, "the bucket pass holds every pivot");
+
 constexpr int kPipeChunks = 8;   // host-buffer sort: copy-in chunks
 static_assert(kPipeChunks <= kMaxChunkRuns, "the bucket sort's chunk table holds every chunk");
 constexpr int kPipeGroups = 10;  // host-buffer sort: bucket groups sorted and copied out in turn
@@ -946,10 +951,42 @@ int pa_partition_radix_u32(uint32_t* a, size_t n, const size_t* k, size_t k_len,
     if (k[i] >= n) return set_error(PA_ERR_ARG, "k[%zu] = %zu is not below n = %zu", i, k[i], n);
     if (i && k[i] < k[i - 1]) return set_error(PA_ERR_ARG, "k[] must be ascending (k[%zu] < k[%zu])", i, i - 1);
   }
-  // A sorted array is partitioned around every k at once (each a[k[i]] is
-  // the k[i]-th smallest, nothing before it is larger, nothing after it is
-  // smaller), so the whole partition is one GPU sort.
-  return pa_sort_u32(a, nullptr, n, opts);
+  // Many k: a sorted array is partitioned around every k at once (each
+  // a[k[i]] is the k[i]-th smallest, nothing before it is larger, nothing
+  // after it is smaller), so the partition is one GPU sort.
+  if (k_len > kPartitionSelectMax) return pa_sort_u32(a, nullptr, n, opts);
+  // A few k: one select per k gives the pivot values, then one pass puts
+  // every key in its bucket among them (pa_partition.cu), about
+  // (20 + 4 k_len) bytes per key against the sort's 36.
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t stream = stream_of(opts);
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+  const bool dev = is_device_ptr(a);
+  const size_t cand_cap = n / 4 + 1024;
+  uint32_t *d_a = nullptr, *tmp = nullptr, *piv = nullptr;
+  void *cand = nullptr, *work = nullptr;
+  unsigned long long* counts = nullptr;
+  auto layout = [&](Carve& c) {
+    d_a = dev ? a : c.take<uint32_t>(n);
+    tmp = c.take<uint32_t>(n);
+    cand = c.take<char>(cand_cap * 4);
+    work = c.take<char>(select_state_bytes());
+    piv = c.take<uint32_t>(kPartitionMaxPivots);
+    counts = c.take<unsigned long long>(partition_scratch_words(n, (int)k_len));
+  };
+  Carve m{nullptr};
+  layout(m);
+  if (int rc = ensure_dev(ws, stream, m.off)) return rc;
+  Carve r{ws->dev};
+  layout(r);
+  if (!dev) PA_CUDA(cudaMemcpyAsync(d_a, a, n * 4, cudaMemcpyHostToDevice, stream));
+  for (size_t i = 0; i < k_len; ++i)
+    PA_CUDA(launch_select(d_a, n, k[i], 4, cand, cand_cap, work, piv + i, ws->err, stream));
+  PA_CUDA(launch_partition(d_a, tmp, n, piv, (int)k_len, counts, stream));
+  PA_CUDA(cudaMemcpyAsync(a, tmp, n * 4, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream));
+  return finish(ws, stream, dev && opts && opts->async_device);
 }
 
 int pa_hist_quanta_u32(const uint32_t* a, size_t l, size_t r, size_t work_quanta, size_t quanta,

@@ -118,6 +118,48 @@ cudaError_t launch_counts_t(const void* keys, size_t n, uint32_t shift0, uint32_
   return cudaGetLastError();
 }
 
+// Several arrays' one-digit histograms in one launch: CTAs walk the
+// flattened list of (job, chunk) items; each chunk is counted in lane-banked
+// shared counters (one copy per lane of an 8-lane group) and added into its
+// job's global counts.
+constexpr int kMultiBlock = 512;
+constexpr int kMultiLanes = 8;
+
+template <typename K>
+__global__ void __launch_bounds__(kMultiBlock) digit_counts_multi_kernel(const HistJob* __restrict__ jobs, int njobs,
+                                                                         uint32_t total_chunks) {
+  __shared__ uint32_t s_h[256 * kMultiLanes];
+  __shared__ int s_job;
+  const uint32_t lane = threadIdx.x % kMultiLanes;
+  for (uint32_t item = blockIdx.x; item < total_chunks; item += gridDim.x) {
+    if (threadIdx.x == 0) {  // the job whose chunks hold `item`: last first_chunk <= item
+      int lo = 0, hi = njobs - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].first_chunk <= item) lo = mid;
+        else hi = mid - 1;
+      }
+      s_job = lo;
+    }
+    for (uint32_t i = threadIdx.x; i < 256 * kMultiLanes; i += kMultiBlock) s_h[i] = 0;
+    __syncthreads();
+    const HistJob J = jobs[s_job];
+    const unsigned long long lo = (unsigned long long)(item - J.first_chunk) * kHistJobChunk;
+    const unsigned long long hi = min(J.n, lo + kHistJobChunk);
+    const K* keys = static_cast<const K*>(J.keys);
+    for (unsigned long long i = lo + threadIdx.x; i < hi; i += kMultiBlock)
+      atomicAdd(&s_h[((uint32_t)(keys[i] >> J.shift) & 255u) * kMultiLanes + lane], 1u);
+    __syncthreads();
+    if (threadIdx.x < 256) {
+      uint32_t sum = 0;
+#pragma unroll
+      for (int j = 0; j < kMultiLanes; ++j) sum += s_h[threadIdx.x * kMultiLanes + j];
+      if (sum) atomicAdd(&J.out[threadIdx.x], (unsigned long long)sum);
+    }
+    __syncthreads();
+  }
+}
+
 // Counts per work quantum over keys[l, r): a CTA covers one chunk that never
 // straddles a quantum boundary; quanta are numbered by absolute index
 // (i / work_quanta) as in HistogramByteComponentsAcrossWorkQuantasQC
@@ -263,6 +305,19 @@ cudaError_t launch_digit_counts(const void* keys, size_t n, int key_bytes, int n
     }
   }
   return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_digit_counts_multi(const HistJob* jobs, int njobs, uint32_t total_chunks, int key_bytes,
+                                      cudaStream_t stream) {
+  if (njobs <= 0 || total_chunks == 0) return cudaSuccess;
+  const unsigned grid = (unsigned)min((size_t)total_chunks, (size_t)device_info().sm_count * 4);
+  if (key_bytes == 4)
+    digit_counts_multi_kernel<uint32_t><<<grid, kMultiBlock, 0, stream>>>(jobs, njobs, total_chunks);
+  else if (key_bytes == 8)
+    digit_counts_multi_kernel<unsigned long long><<<grid, kMultiBlock, 0, stream>>>(jobs, njobs, total_chunks);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_quanta_counts(const uint32_t* keys, size_t l, size_t r, size_t work_quanta,

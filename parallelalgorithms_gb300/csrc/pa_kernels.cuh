@@ -58,6 +58,22 @@ cudaError_t launch_digit_counts(const void* keys, size_t n, int key_bytes, int n
                                 uint32_t shift0, uint32_t shift_step, bool is_float, unsigned long long* out,
                                 cudaStream_t stream);
 
+// Several arrays' 256-bin histograms of (key >> shift) & 255 in one launch
+// (the serving loop's coalesced histogram requests).  jobs[0, njobs) in
+// device memory; job j's keys are split into kHistJobChunk-key chunks
+// numbered from first_chunk on (first_chunk ascending, total_chunks in all);
+// counts are ADDED into each job's out[256].  key_bytes 4 or 8.
+constexpr uint32_t kHistJobChunk = 64 * 1024;
+struct HistJob {
+  const void* keys;
+  unsigned long long n;
+  unsigned long long* out;
+  uint32_t shift;
+  uint32_t first_chunk;
+};
+cudaError_t launch_digit_counts_multi(const HistJob* jobs, int njobs, uint32_t total_chunks, int key_bytes,
+                                      cudaStream_t stream);
+
 // Byte counting sort's second step: a[0, n) = each byte value v repeated
 // counts[v] times, in value order (counts: 256 words summing to n).
 cudaError_t launch_counting_fill(uint8_t* a, size_t n, const unsigned long long* counts, cudaStream_t stream);
@@ -189,6 +205,17 @@ cudaError_t launch_sum(const void* keys, size_t n, int elem_kind, unsigned long 
 // *total (zeroed by the caller) += every chunk's sum, modulo 2^64.
 cudaError_t launch_sum_chunks(const void* keys, size_t n, int elem_kind, size_t chunk, unsigned long long* sums,
                               unsigned long long* total, cudaStream_t stream);
+
+// ---- partition around a few k (pa_partition.cu) ---------------------------
+// Most pivots one partition handles: 2 * 7 + 1 = 15 buckets fit 4 bits.
+constexpr int kPartitionMaxPivots = 7;
+// out[0, n) = in[0, n) arranged in the 2m + 1 buckets defined by the m sorted
+// pivots (device): below pivot 0, equal to it, between pivots 0 and 1, ...,
+// above the last one; the order inside a bucket is not specified.  scratch
+// holds partition_scratch_words(n, m) words.  in and out must not overlap.
+size_t partition_scratch_words(size_t n, int m);
+cudaError_t launch_partition(const uint32_t* in, uint32_t* out, size_t n, const uint32_t* pivots, int m,
+                             unsigned long long* scratch, cudaStream_t stream);
 
 // ---- select (pa_select.cu) -------------------------------------------------
 struct SelectState;

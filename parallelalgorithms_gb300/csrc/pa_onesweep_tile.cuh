@@ -3,6 +3,8 @@
 // (pa_segmented.cu).  See pa_onesweep.cu for the algorithm.
 #pragma once
 
+#include <type_traits>
+
 #include "pa_common.cuh"
 #include "pa_kernels.cuh"
 
@@ -591,11 +593,16 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
   uint32_t rk[(ITEMS + 1) / 2];  // in-warp ranks (< 32 * ITEMS), two 16-bit halves per word
 #pragma unroll
   for (int q = 0; q < (ITEMS + 1) / 2; ++q) rk[q] = 0;
-  auto rank_item = [&](auto jc) {
-    constexpr int j = decltype(jc)::value;
+  // all of the warp's keys into registers first, so that no item's counter
+  // chain starts with a shared-memory load
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
     const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
     k[j] = s_keys[idx];
     if (HAS_VALS) v[j] = s_vals[idx];
+  }
+  auto rank_item = [&](auto jc) {
+    constexpr int j = decltype(jc)::value;
     const uint32_t d = digit8(k[j], dsel, dupper);
 #if PA_MATCH_ATOMIC_OR || PA_MATCH_MIX
     constexpr bool kSmemMatch = PA_MATCH_ATOMIC_OR || (PA_MATCH_MIX > 0 && j % (PA_MATCH_MIX > 0 ? PA_MATCH_MIX : 1) == 0);
@@ -752,6 +759,292 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
     scatter([](K x) { return from_ordered(x, true); });
   else
     scatter([](K x) { return x; });
+}
+
+// ---------------------------------------------------------------------------
+// Wide-digit tile: the multisplit tile for RB-bit digits with RB > 8 (11:
+// 2048 bins, three passes for 32-bit keys).  Same steps as the 8-bit body
+// above, with what changes when a tile has 2048 bins:
+//   - the peers of a key come from RB ballots (no shared-memory match words:
+//     [warps][2048] of them would not fit next to the counters);
+//   - the warps' counters are 16-bit ([warps][2048] x 2 bytes; a warp's count
+//     and the in-tile starts folded into it stay below 2^16);
+//   - the per-bin scans, the in-tile bin starts and the look-back loop over
+//     the bins, each thread owning 2048 / BLOCK of them (its look-back walks
+//     them in lockstep, their loads in flight together);
+//   - the digit is (key >> shift) & (2^RB - 1).
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int RB>
+struct WideGeometry {
+  static constexpr int kWarps = BLOCK / 32;
+  static constexpr int kTile = BLOCK * ITEMS;
+  static constexpr int kBins = 1 << RB;
+  static constexpr size_t kKeysOff = 0;
+  static constexpr size_t kValsOff = kKeysOff + (size_t)kTile * sizeof(K);
+  static constexpr size_t kWhOff = kValsOff + (HAS_VALS ? (size_t)kTile * 4 : 0);          // [warps][bins] u16
+  static constexpr size_t kBaseOff = kWhOff + (((size_t)kWarps * kBins * 2 + 15) & ~(size_t)15);  // [bins] 8 B
+  static constexpr size_t kTstartOff = kBaseOff + (size_t)kBins * 8;                          // [bins] u32
+  static constexpr size_t kTcountOff = kTstartOff + (size_t)kBins * 4;                        // [bins] u32
+  static constexpr size_t kWarpTotOff = kTcountOff + (size_t)kBins * 4;                       // [warps] u32
+  static constexpr size_t kBarOff = kWarpTotOff + (((size_t)kWarps * 4 + 7) & ~(size_t)7);
+  static constexpr size_t kTileIdOff = kBarOff + 8;
+  static constexpr size_t kAbortOff = kTileIdOff + 4;
+  static constexpr size_t kBytes = kAbortOff + 4;
+  static_assert(kBins % BLOCK == 0, "every thread owns the same number of bins");
+  static_assert(kTile + 32 * ITEMS < 65536, "16-bit counters hold in-tile positions");
+  static_assert(kTile % 4 == 0 && kValsOff % 16 == 0, "tile buffers stay 16-byte aligned");
+};
+
+// Lanes whose RB-bit digit equals this lane's, from RB ballots.
+template <int RB>
+__device__ __forceinline__ uint32_t match_bits(uint32_t d) {
+  uint32_t peers = 0xFFFFFFFFu;
+  static_for<RB>([&](auto bc) {
+    constexpr uint32_t B = 1u << decltype(bc)::value;
+    asm("{\n\t.reg .pred p;\n\t.reg .b32 t;\n\t"
+        "and.b32 t, %1, %2;\n\t"
+        "setp.ne.u32 p, t, 0;\n\t"
+        "vote.sync.ballot.b32 t, p, 0xffffffff;\n\t"
+        "@!p not.b32 t, t;\n\t"
+        "and.b32 %0, %0, t;\n\t}"
+        : "+r"(peers)
+        : "r"(d), "n"(B));
+  });
+  return peers;
+}
+
+template <int RB, typename K>
+__device__ __forceinline__ uint32_t digit_wide(K key, uint32_t shift) {
+  return (uint32_t)(key >> shift) & ((1u << RB) - 1u);
+}
+
+// One wide-digit tile in the WideGeometry layout at `smem`: starts its bulk
+// copy (thread 0) and sorts, publishes and writes it out.  Called by all
+// BLOCK threads after a barrier that ends every earlier use of `smem`.
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int RB, typename S>
+__device__ __forceinline__ void onesweep_tile_wide(const TileJob<K, S>& job, unsigned char* smem, uint64_t* s_bar,
+                                                   uint32_t& parity) {
+  using G = WideGeometry<K, HAS_VALS, BLOCK, ITEMS, RB>;
+  using SW = StatusWord<S>;
+  constexpr int TILE = G::kTile;
+  constexpr int WARPS = G::kWarps;
+  constexpr int R = G::kBins;
+  constexpr int BPT = R / BLOCK;  // bins per thread
+  constexpr uint32_t FULL = 0xFFFFFFFFu;
+  K* s_keys = reinterpret_cast<K*>(smem + G::kKeysOff);
+  uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + G::kValsOff);
+  uint16_t* s_wh = reinterpret_cast<uint16_t*>(smem + G::kWhOff);
+  S* s_base = reinterpret_cast<S*>(smem + G::kBaseOff);
+  uint32_t* s_tstart = reinterpret_cast<uint32_t*>(smem + G::kTstartOff);
+  uint32_t* s_tcount = reinterpret_cast<uint32_t*>(smem + G::kTcountOff);
+  uint32_t* s_warp = reinterpret_cast<uint32_t*>(smem + G::kWarpTotOff);
+  uint32_t* s_abort = reinterpret_cast<uint32_t*>(smem + G::kAbortOff);
+
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+  const uint32_t tile = job.tile;
+  const size_t tile_base = (size_t)tile * TILE;
+  const uint32_t tile_n = (uint32_t)min((size_t)TILE, job.n - tile_base);
+  const uint32_t shift = job.shift;
+  if (tid == 0) {
+    *s_abort = 0;
+    tile_issue_load<K, HAS_VALS, TILE>(job, tile, s_keys, s_vals, s_bar);
+  }
+  uint32_t* wh_words = reinterpret_cast<uint32_t*>(s_wh);
+  for (uint32_t i = tid; i < (uint32_t)(WARPS * R / 2); i += BLOCK) wh_words[i] = 0;
+  const bool tma_ok = tile_tma_ok<K, HAS_VALS>(job);
+  uint32_t loaded = 0;
+  if (tma_ok) {
+    loaded = ((tile_n * (uint32_t)sizeof(K)) & ~15u) / (uint32_t)sizeof(K);
+    if (HAS_VALS)
+      for (uint32_t i = ((tile_n * 4u) & ~15u) / 4u + tid; i < tile_n; i += BLOCK) s_vals[i] = job.vin[tile_base + i];
+  } else if (HAS_VALS) {
+    for (uint32_t i = tid; i < tile_n; i += BLOCK) s_vals[i] = job.vin[tile_base + i];
+  }
+  for (uint32_t i = loaded + tid; i < tile_n; i += BLOCK) s_keys[i] = job.in[tile_base + i];
+  // a short last tile is padded with all-ones keys (see the 8-bit body)
+  for (uint32_t i = tile_n + tid; i < (uint32_t)TILE; i += BLOCK) s_keys[i] = ~(K)0;
+  bool tma_pending = false;
+  if (tma_ok) {
+    tma_pending = !mbar_wait_bounded(s_bar, parity, job.err);
+    if (tma_pending) *s_abort = 1;
+    parity ^= 1u;
+  }
+  __syncthreads();
+  if (job.tin) {
+    order_tile_in_place<K, BLOCK>(s_keys, tile_n);
+    __syncthreads();
+  }
+
+  // rank within the warp
+  const uint32_t lt = lanemask_lt();
+  const uint32_t wbase = warp * ITEMS * 32;
+  uint16_t* wh = s_wh + warp * R;
+  K k[ITEMS];
+  uint32_t v[HAS_VALS ? ITEMS : 1];
+  uint32_t rk[(ITEMS + 1) / 2];
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
+    k[j] = s_keys[idx];
+    if (HAS_VALS) v[j] = s_vals[idx];
+  }
+#pragma unroll
+  for (int q = 0; q < (ITEMS + 1) / 2; ++q) rk[q] = 0;
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    const uint32_t d = digit_wide<RB>(k[j], shift);
+    const uint32_t peers = match_bits<RB>(d);
+    const uint32_t pl = peers & lt;
+    const uint32_t base = wh[d];
+    __syncwarp();
+    if (pl == 0) wh[d] = (uint16_t)(base + __popc(peers));
+    rk[j / 2] |= (base + __popc(pl)) << (16 * (j % 2));
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // per bin: exclusive scan over the warps, tile count, publish
+#pragma unroll
+  for (int m = 0; m < BPT; ++m) {
+    const uint32_t b = tid + (uint32_t)m * BLOCK;
+    uint32_t sum = 0;
+#pragma unroll 4
+    for (int w = 0; w < WARPS; ++w) {
+      const uint32_t c = s_wh[w * R + b];
+      s_wh[w * R + b] = (uint16_t)sum;
+      sum += c;
+    }
+    s_tcount[b] = sum;
+    st_relaxed_gpu(job.status + (size_t)tile * R + b, (S)((tile == 0 ? SW::kIncl : SW::kAgg) | (S)sum));
+  }
+  __syncthreads();
+  {  // in-tile bin starts: thread t scans bins [t * BPT, (t + 1) * BPT)
+    uint32_t c[BPT];
+    uint32_t local = 0;
+#pragma unroll
+    for (int i = 0; i < BPT; ++i) {
+      c[i] = s_tcount[tid * BPT + i];
+      local += c[i];
+    }
+    uint32_t run = block_exclusive_scan<BLOCK>(local, s_warp);
+#pragma unroll
+    for (int i = 0; i < BPT; ++i) {
+      s_tstart[tid * BPT + i] = run;
+      run += c[i];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < BPT; ++m) {  // fold the in-tile start of each bin into the warp offsets
+    const uint32_t b = tid + (uint32_t)m * BLOCK;
+    const uint32_t ts = s_tstart[b];
+#pragma unroll 4
+    for (int w = 0; w < WARPS; ++w) s_wh[w * R + b] = (uint16_t)(s_wh[w * R + b] + ts);
+  }
+  __syncthreads();
+
+  // stage keys at their in-tile sorted position; then the look-back
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    const uint32_t pos = wh[digit_wide<RB>(k[j], shift)] + ((rk[j / 2] >> (16 * (j % 2))) & 0xFFFFu);
+    s_keys[pos] = k[j];
+    if (HAS_VALS) s_vals[pos] = v[j];
+  }
+  {
+    S excl[BPT];
+#pragma unroll
+    for (int m = 0; m < BPT; ++m) excl[m] = 0;
+    if (tile > 0) {
+      long long t[BPT];
+      bool done[BPT];
+#pragma unroll
+      for (int m = 0; m < BPT; ++m) {
+        t[m] = (long long)tile - 1;
+        done[m] = false;
+      }
+      uint32_t spins = 0;
+      bool all_done = false;
+      while (!all_done) {
+        S sw[BPT][kLookbackWidth];
+#pragma unroll
+        for (int m = 0; m < BPT; ++m) {
+          const S* base = job.status + tid + (size_t)m * BLOCK;
+#pragma unroll
+          for (int i = 0; i < kLookbackWidth; ++i)
+            sw[m][i] = (!done[m] && t[m] - i >= 0) ? ld_relaxed_gpu(base + (size_t)(t[m] - i) * R) : (S)SW::kIncl;
+        }
+        bool progress = false;
+        all_done = true;
+#pragma unroll
+        for (int m = 0; m < BPT; ++m) {
+          if (!done[m]) {
+            int used = 0;
+#pragma unroll
+            for (int i = 0; i < kLookbackWidth; ++i) {
+              if (done[m] || used != i) break;
+              const uint32_t flag = (uint32_t)(sw[m][i] >> SW::kShift);
+              if (flag == 0) break;
+              excl[m] += sw[m][i] & SW::kMask;
+              ++used;
+              if (flag == 2u) done[m] = true;
+            }
+            t[m] -= used;
+            progress |= used > 0;
+          }
+          all_done &= done[m];
+        }
+        if (!all_done && !progress) {
+          ++spins;
+          if (spins > job.spin_limit || ((spins & 1023u) == 0 && ld_relaxed_gpu(job.err) != 0)) {
+            raise_error(job.err, DEVERR_LOOKBACK_TIMEOUT);
+            *s_abort = 1;
+            break;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < BPT; ++m) {
+      const uint32_t b = tid + (uint32_t)m * BLOCK;
+      if (tile > 0)  // published even after a timeout, so that no successor waits on this tile
+        st_relaxed_gpu(job.status + (size_t)tile * R + b, (S)(SW::kIncl | (excl[m] + (S)s_tcount[b])));
+      s_base[b] = (S)job.bin_start[b] + excl[m] - (S)s_tstart[b];
+    }
+  }
+  __syncthreads();
+
+  // write out in bin-contiguous runs (nothing after a failed wait)
+  if (*s_abort) {
+    if (tma_pending) mbar_wait_bounded(s_bar, parity ^ 1u, job.err);
+    return;
+  }
+  const S n_out = (S)job.n;
+  const bool full = tile_n == (uint32_t)TILE;
+  auto scatter = [&](auto toutc) {
+    constexpr bool TOUT = decltype(toutc)::value;
+    if (full) {
+#pragma unroll 4
+      for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t i = (uint32_t)j * BLOCK + tid;
+        const K key = s_keys[i];
+        const S o = s_base[digit_wide<RB>(key, shift)] + i;
+        job.out[o] = TOUT ? from_ordered(key, true) : key;
+        if (HAS_VALS) job.vout[o] = s_vals[i];
+      }
+    } else {
+      for (uint32_t i = tid; i < tile_n; i += BLOCK) {
+        const K key = s_keys[i];
+        const S o = s_base[digit_wide<RB>(key, shift)] + i;
+        if (o < n_out) {
+          job.out[o] = TOUT ? from_ordered(key, true) : key;
+          if (HAS_VALS) job.vout[o] = s_vals[i];
+        }
+      }
+    }
+  };
+  if (job.tout)
+    scatter(std::true_type{});
+  else
+    scatter(std::false_type{});
 }
 
 // One multisplit tile in the Geometry layout (one tile buffer at offset 0):

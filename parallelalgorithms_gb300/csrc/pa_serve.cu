@@ -1,7 +1,9 @@
 // Serving loop: sort / select / histogram requests arrive on any thread, are
 // admitted against an HBM budget, run with their data device-resident, and
-// complete asynchronously, with waiting 32-bit sorts coalesced into one
-// batched launch (the persistent segmented-sort kernel).  Scheduling policy:
+// complete asynchronously.  Waiting requests of one kind share a unit:
+// 32-bit sorts one batched launch (the persistent segmented-sort kernel),
+// histograms one launch over all their arrays, 64-bit sorts and selects one
+// allocation, stream and completion event.  Scheduling policy:
 // pa_serve_core.h; this file is its CUDA backend and the C ABI.
 //
 // No reference counterpart (the reference has no serving path; its nearest
@@ -137,27 +139,23 @@ class GpuBackend {
     return f;
   }
 
+  // 32-bit sorts of a shared unit run as one segmented-sort launch.
+  static bool segmented(const Unit& u) {
+    return u.batched && u.reqs[0]->op == OP_SORT && u.reqs[0]->key_bytes == 4;
+  }
+  // Bytes of one request's result slot: the select's key (8, zero-extended)
+  // or the histogram's 256 counts.
+  static size_t result_slot(int op) { return op == OP_SELECT ? 8 : op == OP_HIST ? 256 * 8 : 0; }
+
   size_t unit_bytes(const Unit& u) {
-    size_t b = 1024;  // error word + result slots
-    if (u.batched) {
+    if (segmented(u)) {
       size_t total = 0;
       for (const Request* r : u.reqs) total += r->n;
       // keys + tmp, plus the plan block (under 1 byte per key for 8192-key tiles)
-      return b + align256(total * 4) * 2 + total + ((size_t)8 << 20);
+      return 1024 + align256(total * 4) * 2 + total + ((size_t)8 << 20);
     }
-    const Request* r = u.reqs[0];
-    const pa_request* q = user_of(r);
-    const size_t kb = (size_t)r->key_bytes;
-    const bool host = !q->internal_device;
-    if (host) b += align256(r->n * kb);
-    switch (r->op) {
-      case OP_SORT: b += align256(r->n * kb) + align256(sort_scratch_bytes(r->n, (int)kb, false)); break;
-      case OP_SELECT: b += align256((r->n / 4 + 1024) * kb) + align256(select_state_bytes()); break;
-      default: b += 256 * 8; break;
-    }
-    return b;
+    return group_layout(u, nullptr, nullptr);
   }
-
   void launch(Unit& u) {
     auto* st = new UnitState();
     u.state = st;
@@ -181,7 +179,7 @@ class GpuBackend {
     cudaError_t e = cudaEventCreateWithFlags(&st->ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&st->dmem), u.bytes, pool_, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(st->dmem, 0, 256, s);  // error word + result slot
-    if (e == cudaSuccess) e = u.batched ? launch_batch(u, st, s) : launch_single(u, st, s);
+    if (e == cudaSuccess) e = segmented(u) ? launch_batch(u, st, s) : launch_group(u, st, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(st->err_host, st->dmem, 4, cudaMemcpyDeviceToHost, s);
     if (st->dmem) {
       const cudaError_t f = cudaFreeAsync(st->dmem, s);
@@ -222,9 +220,10 @@ class GpuBackend {
     // results land in page-locked memory first (a device-to-host copy into the
     // caller's pageable array would make the launching thread wait for the
     // unit's work); they move to the caller's array now that the work is done
-    if (status == PA_OK && st->result_host && u.reqs.size() == 1) {
-      const Request* r = u.reqs[0];
-      std::memcpy(user_of(r)->result, st->result_host, r->op == OP_SELECT ? 8 : 256 * 8);
+    if (status == PA_OK && st->result_host) {
+      const size_t slot = result_slot(u.reqs[0]->op);
+      for (size_t i = 0; i < u.reqs.size(); ++i)
+        std::memcpy(user_of(u.reqs[i])->result, static_cast<char*>(st->result_host) + i * slot, slot);
     }
     for (Request* r : u.reqs) r->status = status;
     if (st->ev) cudaEventDestroy(st->ev);
@@ -239,48 +238,90 @@ class GpuBackend {
   double now() { return now_s(); }
 
  private:
-  // Layout of a single-request unit: [err+result 256][keys][tmp / cand][scratch]
-  cudaError_t launch_single(Unit& u, UnitState* st, cudaStream_t s) {
-    Request* r = u.reqs[0];
-    pa_request* q = user_of(r);
-    const size_t kb = (size_t)r->key_bytes;
-    char* base = st->dmem;
-    uint32_t* err = reinterpret_cast<uint32_t*>(base);
-    void* result = base + 8;  // 8-byte select result
-    size_t off = 256;
-    void* keys = q->keys;
-    const bool host = !q->internal_device;
+  // A unit of requests of one kind (one request, or a shared unit of 64-bit
+  // sorts, selects or histograms), laid out in one device block:
+  //   [error word 256][result slots][histogram job table][per request: keys
+  //   (host buffers only), then tmp + sort scratch, or the select's
+  //   candidates + state].
+  // Measures the block (dmem == nullptr, returns its bytes) or enqueues the
+  // unit's copies and kernels on `s` with that layout.  Requests of a unit
+  // run one after another on its stream; the histograms of a unit are counted
+  // by one launch over all of their arrays.
+  size_t group_layout(const Unit& u, UnitState* st, cudaStream_t s, cudaError_t* err_out = nullptr) {
+    const Request* h = u.reqs[0];
+    const int op = h->op;
+    const size_t kb = (size_t)h->key_bytes;
+    const size_t cnt = u.reqs.size();
+    const size_t slot = result_slot(op);
+    char* base = st ? st->dmem : nullptr;
+    const bool run = base != nullptr;
     cudaError_t e = cudaSuccess;
-    if (host) {
-      keys = base + off;
-      off += align256(r->n * kb);
-      e = cudaMemcpyAsync(keys, q->keys, r->n * kb, cudaMemcpyHostToDevice, s);
+    uint32_t* err = reinterpret_cast<uint32_t*>(base);
+    size_t off = 256;
+    char* results = base + off;
+    off += align256(slot * cnt);
+    HistJob* jobs = reinterpret_cast<HistJob*>(base + off);
+    if (op == OP_HIST) off += align256(sizeof(HistJob) * cnt);
+    std::vector<HistJob> hj;
+    uint32_t chunks = 0;
+    if (run && slot) {
+      st->result_host = take_pinned(slot * cnt);
+      if (!st->result_host) e = cudaErrorMemoryAllocation;
+      if (e == cudaSuccess) e = cudaMemsetAsync(results, 0, slot * cnt, s);
     }
-    if (e != cudaSuccess) return e;
-    if (r->op == OP_SORT) {
-      void* tmp = base + off;
-      off += align256(r->n * kb);
-      SortScratch sc{};
-      sort_scratch_layout(base + off, r->n, (int)kb, false, &sc);
-      e = enqueue_sort(sc, keys, tmp, nullptr, nullptr, r->n, (int)kb, false, err, s);
-      if (e == cudaSuccess && host) e = cudaMemcpyAsync(q->keys, keys, r->n * kb, cudaMemcpyDeviceToHost, s);
-    } else if (r->op == OP_SELECT) {
-      st->result_host = take_pinned(8);
-      if (!st->result_host) return cudaErrorMemoryAllocation;
-      const size_t cap = r->n / 4 + 1024;
-      void* cand = base + off;
-      off += align256(cap * kb);
-      void* work = base + off;
-      e = launch_select(keys, r->n, q->k, (int)kb, cand, cap, work, result, err, s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(st->result_host, result, 8, cudaMemcpyDeviceToHost, s);
-    } else {
-      st->result_host = take_pinned(256 * 8);
-      if (!st->result_host) return cudaErrorMemoryAllocation;
-      auto* counts = reinterpret_cast<unsigned long long*>(base + off);
-      e = cudaMemsetAsync(counts, 0, 256 * 8, s);
-      if (e == cudaSuccess) e = launch_digit_counts(keys, r->n, (int)kb, 1, 8, q->shift, 0, false, counts, s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(st->result_host, counts, 256 * 8, cudaMemcpyDeviceToHost, s);
+    for (size_t i = 0; i < cnt && e == cudaSuccess; ++i) {
+      const Request* r = u.reqs[i];
+      pa_request* q = user_of(r);
+      const bool host = !q->internal_device;
+      void* keys = q->keys;
+      if (host) {
+        keys = base + off;
+        off += align256(r->n * kb);
+        if (run) e = cudaMemcpyAsync(keys, q->keys, r->n * kb, cudaMemcpyHostToDevice, s);
+      }
+      if (op == OP_SORT) {
+        void* tmp = base + off;
+        off += align256(r->n * kb);
+        char* scratch = base + off;
+        off += align256(sort_scratch_bytes(r->n, (int)kb, false));
+        if (run && e == cudaSuccess) {
+          SortScratch sc{};
+          sort_scratch_layout(scratch, r->n, (int)kb, false, &sc);
+          e = enqueue_sort(sc, keys, tmp, nullptr, nullptr, r->n, (int)kb, false, err, s);
+          if (e == cudaSuccess && host) e = cudaMemcpyAsync(q->keys, keys, r->n * kb, cudaMemcpyDeviceToHost, s);
+        }
+      } else if (op == OP_SELECT) {
+        const size_t cap = r->n / 4 + 1024;
+        void* cand = base + off;
+        off += align256(cap * kb);
+        void* work = base + off;
+        off += align256(select_state_bytes());
+        if (run && e == cudaSuccess) e = launch_select(keys, r->n, q->k, (int)kb, cand, cap, work, results + i * slot, err, s);
+      } else {
+        hj.push_back({keys, (unsigned long long)r->n, reinterpret_cast<unsigned long long*>(results + i * slot),
+                      q->shift, chunks});
+        chunks += (uint32_t)((r->n + kHistJobChunk - 1) / kHistJobChunk);
+      }
     }
+    if (run && e == cudaSuccess && op == OP_HIST) {
+      // the job table goes up from page-locked memory (see launch_batch)
+      st->staging = take_pinned(sizeof(HistJob) * cnt);
+      if (!st->staging) e = cudaErrorMemoryAllocation;
+      if (e == cudaSuccess) {
+        std::memcpy(st->staging, hj.data(), sizeof(HistJob) * cnt);
+        e = cudaMemcpyAsync(jobs, st->staging, sizeof(HistJob) * cnt, cudaMemcpyHostToDevice, s);
+      }
+      if (e == cudaSuccess) e = launch_digit_counts_multi(jobs, (int)cnt, chunks, (int)kb, s);
+    }
+    if (run && e == cudaSuccess && slot)
+      e = cudaMemcpyAsync(st->result_host, results, slot * cnt, cudaMemcpyDeviceToHost, s);
+    if (err_out) *err_out = e;
+    return off + 1024;
+  }
+
+  cudaError_t launch_group(Unit& u, UnitState* st, cudaStream_t s) {
+    cudaError_t e = cudaSuccess;
+    group_layout(u, st, s, &e);
     return e;
   }
 

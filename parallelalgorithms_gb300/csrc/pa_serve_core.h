@@ -1,8 +1,11 @@
 // Scheduling core of the serving loop: requests arrive on any thread, wait in
 // FIFO order, are admitted while their device memory fits the configured HBM
 // budget (and the memory the device reports free), are grouped into units --
-// waiting 32-bit sort requests are coalesced into one batched launch -- and
-// retire when their unit's device work has finished.
+// the head request and the waiting requests of the same kind (operation and
+// key width) share one unit: 32-bit sorts one persistent segmented-sort
+// launch, histograms one multi-array histogram launch, 64-bit sorts and
+// selects one allocation, stream and completion event -- and retire when
+// their unit's device work has finished.
 //
 // Header-only and free of CUDA: the device side is a Backend with
 //   size_t free_bytes();                  device memory free right now
@@ -43,8 +46,8 @@ struct Request {
 };
 
 struct Unit {
-  std::vector<Request*> reqs;
-  bool batched = false;  // coalesced 32-bit sorts sharing one launch
+  std::vector<Request*> reqs;  // all of one kind (operation and key width)
+  bool batched = false;        // more than one request
   size_t bytes = 0;
   int lane = -1;         // backend stream slot
   void* state = nullptr;
@@ -54,7 +57,10 @@ struct Config {
   size_t budget_bytes = (size_t)64 << 30;
   int max_inflight = 4;             // units on the device at once
   int max_batch_requests = 256;     // requests coalesced into one launch
-  size_t max_batch_keys = (size_t)1 << 28;
+  size_t max_batch_keys = (size_t)1 << 28;   // keys of a segmented (32-bit sort) unit
+  size_t max_group_keys = (size_t)1 << 24;   // keys of any other shared unit: its requests run
+                                             // one after another, so large ones stay alone and
+                                             // overlap on the other streams
   size_t window = 1024;             // waiting requests scanned for coalescing
   bool coalesce = true;
 };
@@ -168,26 +174,30 @@ class Scheduler {
   }
 
  private:
-  bool coalescible(const Request* r) const { return cfg_.coalesce && r->op == OP_SORT && r->key_bytes == 4; }
+  // 32-bit sorts share one persistent segmented-sort launch; other kinds
+  // share an allocation, a stream and (histograms) one launch.
+  static bool segmented(const Request* r) { return r->op == OP_SORT && r->key_bytes == 4; }
+  static bool same_kind(const Request* a, const Request* b) { return a->op == b->op && a->key_bytes == b->key_bytes; }
 
   bool fits(size_t bytes) {
     if (in_use_ + bytes > cfg_.budget_bytes) return false;
     return bytes <= b_.free_bytes();
   }
 
-  // The head request, plus (for a coalescible head) the coalescible requests
-  // found among the next `window` waiting ones, in arrival order.
+  // The head request, plus the requests of its kind found among the next
+  // `window` waiting ones, in arrival order, up to the unit's key limit.
   Unit next_unit() {
     Unit u;
     Request* head = waiting_.front();
     u.reqs.push_back(head);
-    if (coalescible(head)) {
+    const size_t limit = segmented(head) ? cfg_.max_batch_keys : cfg_.max_group_keys;
+    if (cfg_.coalesce && head->n < limit) {
       size_t keys = head->n;
       size_t scanned = 0;
       for (auto it = std::next(waiting_.begin()); it != waiting_.end() && scanned < cfg_.window; ++it, ++scanned) {
         if ((int)u.reqs.size() >= cfg_.max_batch_requests) break;
-        if (!coalescible(*it)) continue;
-        if (keys + (*it)->n > cfg_.max_batch_keys) continue;
+        if (!same_kind(head, *it)) continue;
+        if (keys + (*it)->n > limit) continue;
         keys += (*it)->n;
         u.reqs.push_back(*it);
       }

@@ -64,34 +64,60 @@ static void run_to_idle(Scheduler<FakeBackend>& s) {
 }
 
 int main() {
-  // 1. coalescing: waiting 32-bit sorts share one unit, others run alone, FIFO head first
+  // 1. coalescing: waiting requests of the head's kind (operation and key
+  // width) share its unit, in arrival order; kinds never mix; FIFO heads
   {
     FakeBackend b;
     Config c;
     c.max_inflight = 8;
     Scheduler<FakeBackend> s(b, c);
     std::vector<Request> rs;
-    rs.push_back(make(OP_SORT, 4, 100));
-    rs.push_back(make(OP_SELECT, 4, 50));
-    rs.push_back(make(OP_SORT, 8, 70));
-    rs.push_back(make(OP_SORT, 4, 30));
-    rs.push_back(make(OP_HIST, 8, 10));
-    rs.push_back(make(OP_SORT, 4, 20));
+    rs.push_back(make(OP_SORT, 4, 100));   // 0
+    rs.push_back(make(OP_SELECT, 4, 50));  // 1
+    rs.push_back(make(OP_SORT, 8, 70));    // 2
+    rs.push_back(make(OP_SORT, 4, 30));    // 3
+    rs.push_back(make(OP_HIST, 8, 10));    // 4
+    rs.push_back(make(OP_SORT, 4, 20));    // 5
+    rs.push_back(make(OP_SELECT, 4, 40));  // 6
+    rs.push_back(make(OP_SELECT, 8, 40));  // 7
+    rs.push_back(make(OP_HIST, 8, 12));    // 8
+    rs.push_back(make(OP_SORT, 8, 60));    // 9
     for (auto& r : rs) s.submit(&r);
     run_to_idle(s);
-    CHECK(b.units.size() == 4);
+    CHECK(b.units.size() == 5);
     CHECK(b.units[0].size() == 3);  // the three 32-bit sorts, arrival order
     CHECK(b.units[0][0] == &rs[0] && b.units[0][1] == &rs[3] && b.units[0][2] == &rs[5]);
-    CHECK(b.units[1].size() == 1 && b.units[1][0] == &rs[1]);
-    CHECK(b.units[2][0] == &rs[2] && b.units[3][0] == &rs[4]);
+    CHECK(b.units[1].size() == 2 && b.units[1][0] == &rs[1] && b.units[1][1] == &rs[6]);  // 32-bit selects
+    CHECK(b.units[2].size() == 2 && b.units[2][0] == &rs[2] && b.units[2][1] == &rs[9]);  // 64-bit sorts
+    CHECK(b.units[3].size() == 2 && b.units[3][0] == &rs[4] && b.units[3][1] == &rs[8]);  // 64-bit histograms
+    CHECK(b.units[4].size() == 1 && b.units[4][0] == &rs[7]);                             // the one 64-bit select
     for (auto& r : rs) {
       CHECK(r.status == ST_OK);
       CHECK(r.t_submit <= r.t_admit && r.t_admit < r.t_done);
     }
-    CHECK(rs[0].unit_size == 3 && rs[1].unit_size == 1);
+    CHECK(rs[0].unit_size == 3 && rs[1].unit_size == 2 && rs[7].unit_size == 1);
     const Stats st = s.stats();
-    CHECK(st.submitted == 6 && st.completed == 6 && st.units == 4 && st.batched_units == 1);
-    CHECK(st.coalesced_requests == 3);
+    CHECK(st.submitted == 10 && st.completed == 10 && st.units == 5 && st.batched_units == 4);
+    CHECK(st.coalesced_requests == 9);
+  }
+  // 1b. a shared unit of a kind other than 32-bit sorts stops at max_group_keys
+  {
+    FakeBackend b;
+    Config c;
+    c.max_inflight = 8;
+    c.max_group_keys = 100;
+    Scheduler<FakeBackend> s(b, c);
+    std::vector<Request> rs;
+    rs.push_back(make(OP_SORT, 8, 60));
+    rs.push_back(make(OP_SORT, 8, 50));   // would exceed 100 keys with the head: next unit
+    rs.push_back(make(OP_SORT, 8, 30));   // fits with the head
+    rs.push_back(make(OP_SORT, 8, 150));  // larger than the limit: alone
+    for (auto& r : rs) s.submit(&r);
+    run_to_idle(s);
+    CHECK(b.units.size() == 3);
+    CHECK(b.units[0].size() == 2 && b.units[0][0] == &rs[0] && b.units[0][1] == &rs[2]);
+    CHECK(b.units[1].size() == 1 && b.units[1][0] == &rs[1]);
+    CHECK(b.units[2].size() == 1 && b.units[2][0] == &rs[3]);
   }
   // 2. coalescing off: every request alone
   {

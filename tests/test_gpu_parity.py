@@ -362,6 +362,39 @@ def test_partition_radix(pa, port, ref, n):
         np.testing.assert_array_equal(c[start + length:], a[start + length:])
 
 
+@pytest.mark.parametrize("nk", [1, 2, 3, 6, 7, 12])
+@pytest.mark.parametrize("dist", ["uniform", "few", "presorted", "constant"])
+def test_partition_radix_select_and_sort_paths(pa, port, torch_cuda, nk, dist):
+    """Up to six k go through one select per k and a bucket pass, more k
+    through a sort: either way every listed a[k] is the oracle's, the parts
+    hold, and the keys are a permutation of the input (host and device)."""
+    n = 300_007
+    rng = np.random.default_rng(nk)
+    a = {"uniform": rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32),
+         "few": rng.integers(0, 5, n, dtype=np.uint32),
+         "presorted": np.arange(n, dtype=np.uint32),
+         "constant": np.full(n, 42, np.uint32)}[dist]
+    ks = np.unique(rng.integers(0, n, nk)).astype(np.uint64)
+    if ks.size < nk:  # keep exactly nk distinct k (repeats are allowed by the contract, but test the count)
+        ks = np.linspace(0, n - 1, nk).astype(np.uint64)
+    srt = np.sort(a)
+    for dev in (False, True):
+        got = a.copy()
+        if dev:
+            t = torch_cuda.from_numpy(got.view(np.int32)).cuda()
+            pa.PartitionRadix(t, n, ks)
+            got = t.cpu().numpy().view(np.uint32)
+        else:
+            pa.PartitionRadix(got, n, ks)
+        for k in ks.tolist():
+            assert got[k] == srt[k], (dev, k)
+            assert np.all(got[:k] <= got[k]) and np.all(got[k + 1:] >= got[k])
+        np.testing.assert_array_equal(np.sort(got), srt)
+    want = port.partition_radix(a, ks)
+    for k in ks.tolist():
+        assert want[k] == srt[k]
+
+
 @pytest.mark.parametrize("n", [1, 2, 100003, 1 << 20])
 def test_radix_leaf_merge_sorts(pa, ref, torch_cuda, n):
     """parallel_merge_sort_hybrid_radix (ParallelMergeSort.h:287) with the

@@ -26,7 +26,13 @@ def test_results_same_alone_and_in_the_mix(pa, port, torch_cuda):
         reqs = serving.run_served(srv, specs, bufs, rate=None)
         st = srv.stats()
     assert st["completed"] == len(specs) and st["rejected"] == 0
-    assert st["batched_units"] >= 1  # waiting 32-bit sorts were coalesced
+    assert st["batched_units"] >= 1  # waiting requests shared units
+    # every kind shared a unit with others of its kind at least once: 32-bit
+    # sorts (one segmented launch), 64-bit sorts and selects (one stream),
+    # histograms (one launch over all their arrays)
+    shared = {(s.op, s.key_kind) for s, r in zip(specs, reqs) if r.c.unit_size > 1}
+    assert (serving.REQ_SORT, serving.KEY_U32) in shared and (serving.REQ_SORT, serving.KEY_U64) in shared
+    assert any(op == serving.REQ_SELECT for op, _ in shared) and any(op == serving.REQ_HISTOGRAM for op, _ in shared)
     for s, r, a, a_sorted, (buf, _, src) in zip(specs, reqs, alone, alone_sorted, bufs):
         assert r.c.status == 0
         want = _oracle_result(port, s, src)
