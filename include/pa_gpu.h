@@ -43,8 +43,10 @@ typedef struct pa_opts {
   int async_device;  /* 1: if every buffer is device memory, return once the work is
                         enqueued; bounded-wait failures are then reported by
                         pa_stream_check(stream) */
-  int digit_bits;    /* radix digit width for sorts: 0 or 8 (the reference's
-                        PowerOfTwoRadix = 256) */
+  int digit_bits;    /* radix digit width of the LSD sorts: 0 or 8 (the
+                        reference's PowerOfTwoRadix = 256; one pass per key
+                        byte) or 11 (2048 bins: 3 passes for 32-bit keys, 6 for
+                        64-bit ones; same result) */
   int reserved[4];   /* must be zero */
 } pa_opts;
 
@@ -99,8 +101,8 @@ int pa_sort_two_phase_u32(uint32_t* a, uint32_t* b, size_t n, const pa_opts* opt
  * PA_KEY_F32; vals / tmp_vals may be NULL): same result, always synchronous,
  * and phase_ms[i] receives the device time in milliseconds of each kernel,
  * from CUDA events recorded between the launches: [0] the one-read digit
- * histogram, [1] the bin-offset scan, [2 + p] digit pass p (one per key
- * byte), [2 + passes] the final copy.  phase_cap bounds the entries written.
+ * histogram, [1] the bin-offset scan, [2 + p] digit pass p (one per
+ * digit), [2 + passes] the final copy.  phase_cap bounds the entries written.
  * GPU form of the per-phase timers the reference keeps commented out in its
  * sort (RadixSortLsdParallel.h:255-258, 287, 307-308). */
 enum { PA_KEY_U32 = 0, PA_KEY_U64 = 1, PA_KEY_F32 = 2 };

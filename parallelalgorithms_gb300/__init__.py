@@ -78,14 +78,14 @@ def _ptr(x):
     return ctypes.c_void_p(_info(x)[0]) if x is not None else None
 
 
-def _opts(*bufs):
+def _opts(*bufs, digit_bits: int = 0):
     stream = None
     for b in bufs:
         if b is not None and _is_torch(b):
             s = _info(b)[3]
             if s is not None:
                 stream = s
-    return _native.opts(stream)
+    return _native.opts(stream, digit_bits=digit_bits)
 
 
 def _offset(x, elems: int, itemsize: int):
@@ -108,16 +108,17 @@ def _kind(dt: np.dtype) -> str:
 # ---------------------------------------------------------------------------
 # sort
 # ---------------------------------------------------------------------------
-def sort(keys, values=None, tmp_keys=None, tmp_values=None, n: int | None = None) -> None:
+def sort(keys, values=None, tmp_keys=None, tmp_values=None, n: int | None = None, digit_bits: int = 8) -> None:
     """Stable ascending LSD radix sort of keys[:n] in place (uint32, uint64 or
     float32 keys, float32 by IEEE total order), moving an optional uint32
-    payload with its key."""
+    payload with its key.  digit_bits: 8 (one pass per key byte, the
+    reference's radix) or 11 (2048 bins, fewer passes; same result)."""
     ptr, size, dt, _ = _info(keys)
     n = size if n is None else n
     if n > size:
         raise ValueError("n exceeds the key buffer")
     k = _kind(dt)
-    o = _opts(keys, values, tmp_keys, tmp_values)
+    o = _opts(keys, values, tmp_keys, tmp_values, digit_bits=0 if digit_bits == 8 else digit_bits)
     if values is None:
         call(f"pa_sort_{k}", ctypes.c_void_p(ptr), _ptr(tmp_keys), n, o)
     else:

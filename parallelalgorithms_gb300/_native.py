@@ -121,10 +121,11 @@ def call(name: str, *args) -> None:
         raise PaError(name, rc, lib().pa_last_error_message().decode())
 
 
-def opts(stream: int | None = None, async_device: bool = False) -> ctypes.POINTER(PaOpts) | None:
-    if stream is None and not async_device:
+def opts(stream: int | None = None, async_device: bool = False, digit_bits: int = 0) -> ctypes.POINTER(PaOpts) | None:
+    if stream is None and not async_device and not digit_bits:
         return None
     o = PaOpts()
     o.stream = stream or None
     o.async_device = 1 if async_device else 0
+    o.digit_bits = digit_bits
     return ctypes.pointer(o)

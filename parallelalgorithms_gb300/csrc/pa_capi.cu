@@ -156,8 +156,8 @@ cudaStream_t stream_of(const pa_opts* o) { return o ? static_cast<cudaStream_t>(
 
 int check_opts(const pa_opts* o) {
   if (!o) return PA_OK;
-  if (o->digit_bits != 0 && o->digit_bits != 8)
-    return set_error(PA_ERR_ARG, "digit_bits must be 0 or 8 (got %d)", o->digit_bits);
+  if (o->digit_bits != 0 && o->digit_bits != 8 && o->digit_bits != 11)
+    return set_error(PA_ERR_ARG, "digit_bits must be 0, 8 or 11 (got %d)", o->digit_bits);
   for (int r : o->reserved)
     if (r != 0) return set_error(PA_ERR_ARG, "pa_opts.reserved must be zero");
   return PA_OK;
@@ -488,7 +488,8 @@ int sort_impl(void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t 
   const bool has_vals = vals != nullptr;
   const bool keys_dev = is_device_ptr(keys);
   const bool tmp_dev = is_device_ptr(tmp);
-  if (!keys_dev && !has_vals && !is_float && !(phase_ms && phase_cap > 0) && n >= kPipeMinKeys &&
+  const int rb = (opts && opts->digit_bits == 11) ? 11 : 8;
+  if (!keys_dev && !has_vals && !is_float && !(phase_ms && phase_cap > 0) && n >= kPipeMinKeys && rb == 8 &&
       pipeline_enabled()) {
     const int rc = pipelined_host_sort(ws, stream, keys, n, kb);
     if (rc == PA_OK) return finish(ws, stream, false);
@@ -512,8 +513,8 @@ int sort_impl(void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t 
       d_vals = vals_dev ? vals : c.take<uint32_t>(n);
       d_tvals = tvals_dev ? tmp_vals : c.take<uint32_t>(n);
     }
-    char* sbase = c.take<char>(sort_scratch_bytes(n, kb, has_vals));
-    sort_scratch_layout(sbase, n, kb, has_vals, &sc);
+    char* sbase = c.take<char>(sort_scratch_bytes(n, kb, has_vals, rb));
+    sort_scratch_layout(sbase, n, kb, has_vals, &sc, rb);
   };
   Carve measure{nullptr};
   layout(measure);
@@ -679,22 +680,25 @@ int sum_impl(const void* a, size_t n, int elem_kind, uint64_t* out, const pa_opt
 
 }  // namespace
 
-size_t sort_scratch_bytes(size_t n, int kb, bool has_vals) {
+size_t sort_scratch_bytes(size_t n, int kb, bool has_vals, int radix_bits) {
   SortScratch s{};
-  return sort_scratch_layout(nullptr, n, kb, has_vals, &s);
+  return sort_scratch_layout(nullptr, n, kb, has_vals, &s, radix_bits);
 }
 
-size_t sort_scratch_layout(char* base, size_t n, int kb, bool has_vals, SortScratch* s) {
-  const int passes = kb;  // 8-bit digits: one pass per key byte
-  const size_t tiles = ceil_div(n, onesweep_tile_keys(kb, has_vals));
+size_t sort_scratch_layout(char* base, size_t n, int kb, bool has_vals, SortScratch* s, int radix_bits) {
+  const int passes = sort_passes(kb, radix_bits);
+  const size_t bins = (size_t)1 << radix_bits;
+  const size_t tiles = ceil_div(n, onesweep_tile_keys(kb, has_vals, radix_bits));
   const size_t sb = onesweep_status_bytes(n);
   Carve c{base};
-  s->counts = c.take<unsigned long long>((size_t)passes * 256);
+  s->radix_bits = radix_bits;
+  s->passes = passes;
+  s->counts = c.take<unsigned long long>((size_t)passes * bins);
   s->zero_begin = reinterpret_cast<char*>(s->counts);
   s->tile_ctr = c.take<uint32_t>(passes);
-  s->status = c.take<char>((size_t)passes * tiles * 256 * sb);
+  s->status = c.take<char>((size_t)passes * tiles * bins * sb);
   s->zero_bytes = (size_t)(base + c.off - s->zero_begin);
-  s->bin_start = c.take<unsigned long long>((size_t)passes * 256);
+  s->bin_start = c.take<unsigned long long>((size_t)passes * bins);
   s->ctrl = c.take<SortCtrl>(1);
   s->tiles = tiles;
   s->status_bytes = sb;
@@ -704,7 +708,9 @@ size_t sort_scratch_layout(char* base, size_t n, int kb, bool has_vals, SortScra
 cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32_t* d_vals, uint32_t* d_tvals,
                          size_t n, int kb, bool is_float, uint32_t* err, cudaStream_t stream,
                          const std::function<cudaError_t()>& mark) {
-  const int passes = kb;
+  const int rb = s.radix_bits;
+  const int passes = s.passes;
+  const size_t bins = (size_t)1 << rb;
   const bool has_vals = d_vals != nullptr;
   auto m = [&]() { return mark ? mark() : cudaSuccess; };
   if (n <= small_sort_max_keys(kb, has_vals)) {  // one CTA, one launch
@@ -718,9 +724,9 @@ cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32
   }
   cudaError_t e = cudaMemsetAsync(s.zero_begin, 0, s.zero_bytes, stream);
   if (e == cudaSuccess) e = m();
-  if (e == cudaSuccess) e = launch_digit_counts(d_keys, n, kb, passes, 8, 0, 8, is_float, s.counts, stream);
+  if (e == cudaSuccess) e = launch_digit_counts(d_keys, n, kb, passes, rb, 0, (uint32_t)rb, is_float, s.counts, stream);
   if (e == cudaSuccess) e = m();
-  if (e == cudaSuccess) e = launch_scan_digits(s.counts, passes, 8, n, is_float, true, s.bin_start, s.ctrl, stream);
+  if (e == cudaSuccess) e = launch_scan_digits(s.counts, passes, rb, n, is_float, true, s.bin_start, s.ctrl, stream);
   if (e == cudaSuccess) e = m();
   for (int p = 0; p < passes && e == cudaSuccess; ++p) {
     OnesweepArgs a{};
@@ -729,11 +735,12 @@ cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32
     a.vals_a = d_vals;
     a.vals_b = d_tvals;
     a.n = n;
-    a.shift = 8u * (uint32_t)p;
+    a.shift = (uint32_t)(rb * p);
     a.pass = p;
     a.is_float = is_float ? 1 : 0;
-    a.bin_start = s.bin_start + (size_t)p * 256;
-    a.status = s.status + (size_t)p * s.tiles * 256 * s.status_bytes;
+    a.radix_bits = rb;
+    a.bin_start = s.bin_start + (size_t)p * bins;
+    a.status = s.status + (size_t)p * s.tiles * bins * s.status_bytes;
     a.tile_counter = s.tile_ctr + p;
     a.ctrl = s.ctrl;
     a.err = err;

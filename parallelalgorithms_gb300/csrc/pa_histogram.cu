@@ -28,10 +28,15 @@ constexpr int kHistBlock = 1024;
 template <typename K>
 constexpr int kVec = 16 / (int)sizeof(K);
 
-// Lane copies per counter: 32 (one bank per lane) while the table fits the
-// 227 KB of shared memory, else 16.
+// Lane copies per counter: the most (32 = one bank per lane, then 16, 8, ...)
+// for which the table fits 160 KB of shared memory.
 template <int ND, int RB>
-constexpr int kLanes = (ND * (1 << RB) * 32 * 4 <= 160 * 1024) ? 32 : 16;
+constexpr int kLanes = (ND * (1 << RB) * 32 * 4 <= 160 * 1024)   ? 32
+                       : (ND * (1 << RB) * 16 * 4 <= 160 * 1024) ? 16
+                       : (ND * (1 << RB) * 8 * 4 <= 160 * 1024)  ? 8
+                       : (ND * (1 << RB) * 4 * 4 <= 160 * 1024)  ? 4
+                       : (ND * (1 << RB) * 2 * 4 <= 160 * 1024)  ? 2
+                                                                  : 1;
 
 template <int ND, int RB>
 constexpr size_t hist_smem_bytes() {
@@ -303,6 +308,11 @@ cudaError_t launch_digit_counts(const void* keys, size_t n, int key_bytes, int n
     } else if (key_bytes == 1 && num_digits == 1) {
       return launch_counts_t<uint8_t, 1, 8>(keys, n, shift0, shift_step, false, out, stream);
     }
+  } else if (radix_bits == 11) {
+    if (key_bytes == 4 && num_digits == 3)
+      return launch_counts_t<uint32_t, 3, 11>(keys, n, shift0, shift_step, is_float, out, stream);
+    if (key_bytes == 8 && num_digits == 6)
+      return launch_counts_t<unsigned long long, 6, 11>(keys, n, shift0, shift_step, false, out, stream);
   }
   return cudaErrorInvalidValue;
 }
@@ -430,9 +440,15 @@ cudaError_t launch_counting_fill(uint8_t* a, size_t n, const unsigned long long*
 cudaError_t launch_scan_digits(const unsigned long long* counts, int passes, int radix_bits, size_t n,
                                bool is_float, bool allow_skip, unsigned long long* bin_start, SortCtrl* ctrl,
                                cudaStream_t stream) {
-  if (passes < 1 || passes > kMaxPasses || radix_bits != 8) return cudaErrorInvalidValue;
-  scan_digits_kernel<256><<<1, kScanBlock, 0, stream>>>(counts, passes, n, is_float ? 1 : 0, allow_skip ? 1 : 0,
-                                                         bin_start, ctrl);
+  if (passes < 1 || passes > kMaxPasses) return cudaErrorInvalidValue;
+  if (radix_bits == 8)
+    scan_digits_kernel<256><<<1, kScanBlock, 0, stream>>>(counts, passes, n, is_float ? 1 : 0, allow_skip ? 1 : 0,
+                                                           bin_start, ctrl);
+  else if (radix_bits == 11)
+    scan_digits_kernel<2048><<<1, kScanBlock, 0, stream>>>(counts, passes, n, is_float ? 1 : 0, allow_skip ? 1 : 0,
+                                                            bin_start, ctrl);
+  else
+    return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 

@@ -11,7 +11,11 @@
 
 namespace pa {
 
-constexpr int kMaxPasses = 8;  // 64-bit keys, 8-bit digits
+constexpr int kMaxPasses = 8;  // 64-bit keys, 8-bit digits (11-bit digits: 6 passes)
+
+// Digit widths of the LSD sorts: 8 bits (the reference's PowerOfTwoRadix =
+// 256) or 11 bits (2048 bins; three passes for 32-bit keys).
+inline int sort_passes(int key_bytes, int radix_bits) { return (8 * key_bytes + radix_bits - 1) / radix_bits; }
 
 // Per-pass control computed on the device from the digit histograms, so the
 // host never waits for them: a pass whose digit puts every key in one bin is
@@ -113,11 +117,12 @@ struct OnesweepArgs {
   uint32_t* err;
   uint32_t spin_limit = 0;  // look-back polls before a tile gives up; 0 = kSpinLimit
   size_t max_ctas = 0;      // CTAs launched; 0 = one per tile (only the wait-expiry self-test sets it)
+  int radix_bits = 8;       // digit width: 8 (256 bins) or 11 (2048 bins)
 };
 
-// Tile geometry chosen for (key_bytes, has_vals); the workspace is sized
-// with it.
-size_t onesweep_tile_keys(int key_bytes, bool has_vals);
+// Tile geometry chosen for (key_bytes, has_vals, radix_bits); the workspace
+// is sized with it.
+size_t onesweep_tile_keys(int key_bytes, bool has_vals, int radix_bits = 8);
 // Bytes of one look-back status word for n keys (4 when n < 2^30, else 8).
 size_t onesweep_status_bytes(size_t n);
 cudaError_t launch_onesweep_pass(const OnesweepArgs& a, int key_bytes, bool has_vals, cudaStream_t stream);
@@ -168,6 +173,8 @@ cudaError_t launch_final_copy(void* keys_a, const void* keys_b, uint32_t* vals_a
 // Per-call scratch of a device-resident sort: digit counts, tile tickets and
 // look-back words (zeroed by enqueue_sort), bin starts, pass control.
 struct SortScratch {
+  int radix_bits;
+  int passes;
   unsigned long long* counts;
   uint32_t* tile_ctr;
   char* status;
@@ -178,9 +185,9 @@ struct SortScratch {
   size_t tiles;
   size_t status_bytes;
 };
-size_t sort_scratch_bytes(size_t n, int key_bytes, bool has_vals);
+size_t sort_scratch_bytes(size_t n, int key_bytes, bool has_vals, int radix_bits = 8);
 // Carves the scratch from `base` (nullptr measures); returns its size.
-size_t sort_scratch_layout(char* base, size_t n, int key_bytes, bool has_vals, SortScratch* s);
+size_t sort_scratch_layout(char* base, size_t n, int key_bytes, bool has_vals, SortScratch* s, int radix_bits = 8);
 // Enqueues the whole sort (memset, histogram, scan, passes, final copy) of
 // device buffers on `stream`; `mark`, when set, runs between launches.
 cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32_t* d_vals, uint32_t* d_tvals,

@@ -85,6 +85,45 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
     onesweep_tile<K, HAS_VALS, BLOCK, ITEMS, S>(job, smem, s_bar, parity);
 }
 
+// Wide-digit pass (11-bit digits, 2048 bins): onesweep_tile_wide.
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB, typename S, int RB>
+__global__ void __launch_bounds__(BLOCK, MINB) onesweep_wide_kernel(const OnesweepArgs args) {
+  using G = WideGeometry<K, HAS_VALS, BLOCK, ITEMS, RB>;
+  constexpr int TILE = G::kTile;
+  const PassCtrl pc = args.ctrl->pass[args.pass];
+  if (pc.skip) return;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + G::kBarOff);
+  uint32_t* s_tile_id = reinterpret_cast<uint32_t*>(smem + G::kTileIdOff);
+  if (threadIdx.x == 0) {  // tile ticket: tiles are taken in launch order
+    *s_tile_id = atomicAdd(args.tile_counter, 1u);
+    mbar_init(s_bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const uint32_t tile = *s_tile_id;
+  if ((size_t)tile >= (args.n + TILE - 1) / TILE) {  // a ticket counter that was not reset
+    if (threadIdx.x == 0) raise_error(args.err, DEVERR_BAD_STATE);
+    return;
+  }
+  TileJob<K, S> job;
+  job.in = static_cast<const K*>(pc.src_is_tmp ? args.keys_b : args.keys_a);
+  job.out = static_cast<K*>(pc.src_is_tmp ? args.keys_a : args.keys_b);
+  job.vin = pc.src_is_tmp ? args.vals_b : args.vals_a;
+  job.vout = pc.src_is_tmp ? args.vals_a : args.vals_b;
+  job.n = args.n;
+  job.tile = tile;
+  job.shift = args.shift;
+  job.tin = args.is_float && pc.transform_in;
+  job.tout = args.is_float && pc.transform_out;
+  job.bin_start = args.bin_start;
+  job.status = static_cast<S*>(args.status);
+  job.err = args.err;
+  job.spin_limit = args.spin_limit ? args.spin_limit : kSpinLimit;
+  uint32_t parity = 0;
+  onesweep_tile_wide<K, HAS_VALS, BLOCK, ITEMS, RB, S>(job, smem, s_bar, parity);
+}
+
 // A whole sort of at most BLOCK * ITEMS keys by one CTA, in shared memory:
 // the keys (and payloads) are read once, sorted by stable 4-bit counting
 // passes over every nibble (each thread owns ITEMS consecutive keys, so
@@ -241,8 +280,46 @@ cudaError_t launch_s(const OnesweepArgs& a, cudaStream_t stream) {
 #define PA_GEOM_CASE(B, I, M) \
   if (g.block == B && g.items == I && g.minb == M) return launch_s<K, HAS_VALS, B, I, M>(a, stream);
 
+// Wide-digit geometries (threads, keys per thread, CTAs per SM), the first
+// one active unless PA_WIDE_GEOMETRY selects another (tuning).  The 16-bit
+// warp counters of 2048 bins take 4 KB per warp.
+constexpr GeomChoice kWide[] = {{512, 8, 2}, {256, 16, 2}, {512, 16, 1}};
+
+int wide_geometry_index() {
+  static const int idx = [] {
+    const char* e = std::getenv("PA_WIDE_GEOMETRY");
+    const int i = e ? std::atoi(e) : 0;
+    return (i >= 0 && i < 3) ? i : 0;
+  }();
+  return idx;
+}
+
+template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB>
+cudaError_t launch_wide_t(const OnesweepArgs& a, cudaStream_t stream) {
+  using G = WideGeometry<K, HAS_VALS, BLOCK, ITEMS, 11>;
+  auto go = [&](auto* kern) {
+    cudaError_t e = ensure_dynamic_smem(kern, G::kBytes);
+    if (e != cudaSuccess) return e;
+    size_t tiles = ceil_div(a.n, (size_t)G::kTile);
+    if (a.max_ctas && a.max_ctas < tiles) tiles = a.max_ctas;
+    kern<<<(unsigned)tiles, BLOCK, G::kBytes, stream>>>(a);
+    return cudaGetLastError();
+  };
+  if (a.n < (1ull << 30)) return go(onesweep_wide_kernel<K, HAS_VALS, BLOCK, ITEMS, MINB, uint32_t, 11>);
+  return go(onesweep_wide_kernel<K, HAS_VALS, BLOCK, ITEMS, MINB, unsigned long long, 11>);
+}
+
+template <typename K, bool HAS_VALS>
+cudaError_t launch_wide(const OnesweepArgs& a, cudaStream_t stream) {
+  const GeomChoice g = kWide[wide_geometry_index()];
+  if (g.block == 512 && g.items == 8) return launch_wide_t<K, HAS_VALS, 512, 8, 2>(a, stream);
+  if (g.block == 256 && g.items == 16) return launch_wide_t<K, HAS_VALS, 256, 16, 2>(a, stream);
+  return launch_wide_t<K, HAS_VALS, 512, 16, 1>(a, stream);
+}
+
 template <typename K, bool HAS_VALS>
 cudaError_t launch_kv(const OnesweepArgs& a, cudaStream_t stream) {
+  if (a.radix_bits == 11) return launch_wide<K, HAS_VALS>(a, stream);
   const GeomChoice g = active_geometry<K, HAS_VALS>();
   if constexpr (sizeof(K) == 4 && !HAS_VALS) {
     PA_GEOM_CASE(512, 16, 2)
@@ -268,7 +345,11 @@ cudaError_t launch_kv(const OnesweepArgs& a, cudaStream_t stream) {
 
 }  // namespace
 
-size_t onesweep_tile_keys(int key_bytes, bool has_vals) {
+size_t onesweep_tile_keys(int key_bytes, bool has_vals, int radix_bits) {
+  if (radix_bits == 11) {
+    const GeomChoice g = kWide[wide_geometry_index()];
+    return (size_t)g.block * g.items;
+  }
   GeomChoice g;
   if (key_bytes == 4)
     g = has_vals ? active_geometry<uint32_t, true>() : active_geometry<uint32_t, false>();
