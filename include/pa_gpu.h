@@ -213,7 +213,8 @@ int pa_sum_chunked(const void* a, size_t n, int elem_kind, size_t chunk, uint64_
 typedef struct pa_segsort_config {
   int small_cutoff;  /* 0 (= 4096), 2048, 4096 or 8192 keys */
   int tile_keys;     /* onesweep tile for longer segments: 0 (= 8192), 4096 or 8192 */
-  int digit_bits;    /* 0 or 8 */
+  int digit_bits;    /* 0 or 8 (four passes), or 11 (three passes of 2048 bins;
+                        the result is copied back from tmp) */
   int use_graph;     /* 1: plan runs replay a captured CUDA graph */
   int reserved[4];   /* must be zero */
 } pa_segsort_config;

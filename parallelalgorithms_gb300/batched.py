@@ -45,7 +45,10 @@ class SegSortChoice:
         return c
 
 
-CANDIDATES = [SegSortChoice(c, t) for c in (2048, 4096, 8192) for t in (4096, 8192)]
+# small/large cutoff x tile with 8-bit digits, and 11-bit digits (three
+# passes of 2048 bins) at the default cutoff
+CANDIDATES = ([SegSortChoice(c, t) for c in (2048, 4096, 8192) for t in (4096, 8192)] +
+              [SegSortChoice(4096, t, 11) for t in (4096, 8192)])
 
 
 def _ptr(x) -> int:

@@ -51,44 +51,69 @@ __device__ __forceinline__ void wait_count(const uint32_t* ctr, uint32_t need, u
   raise_error(err, DEVERR_LOOKBACK_TIMEOUT);
 }
 
+// Lane copies of each HIST counter: the 8-bit table (4 x 256) keeps 8, the
+// 11-bit one (3 x 2048) 2, so that both fit shared memory.
+template <int RB>
+__host__ __device__ constexpr int hist_lanes() { return RB == 11 ? 2 : kHistLanes; }
+
+template <int RB>
 __device__ __forceinline__ void hist_item(const PlanDev& P, const Item& it, unsigned char* smem) {
-  const LargeSeg L = P.large[it.seg];
+  constexpr uint32_t D = RB == 11 ? 3u : 4u, R = 1u << RB;
+  constexpr uint32_t L = hist_lanes<RB>();
+  const LargeSeg L_ = P.large[it.seg];
   uint32_t* h = reinterpret_cast<uint32_t*>(smem);
-  constexpr uint32_t kWords = 4 * 256 * kHistLanes;
+  constexpr uint32_t kWords = D * R * L;
   for (uint32_t i = threadIdx.x; i < kWords; i += kBlock) h[i] = 0;
   __syncthreads();
   const uint32_t lo = it.idx * kHistChunk;
-  const uint32_t len = min(kHistChunk, L.len - lo);
-  const uint32_t* src = P.keys + L.base + lo;
-  uint32_t* my = h + (threadIdx.x % kHistLanes);
+  const uint32_t len = min(kHistChunk, L_.len - lo);
+  const uint32_t* src = P.keys + L_.base + lo;
+  uint32_t* my = h + (threadIdx.x % L);
   for (uint32_t i = threadIdx.x; i < len; i += kBlock) {
     const uint32_t k = src[i];
 #pragma unroll
-    for (int d = 0; d < 4; ++d) atomicAdd(my + ((uint32_t)d * 256 + ((k >> (8 * d)) & 255u)) * kHistLanes, 1u);
+    for (uint32_t d = 0; d < D; ++d) atomicAdd(my + (d * R + ((k >> (RB * d)) & (R - 1))) * L, 1u);
   }
   __syncthreads();
-  for (uint32_t e = threadIdx.x; e < 4 * 256; e += kBlock) {
+  for (uint32_t e = threadIdx.x; e < D * R; e += kBlock) {
     uint32_t sum = 0;
 #pragma unroll
-    for (int j = 0; j < kHistLanes; ++j) sum += h[e * kHistLanes + ((j + e) % kHistLanes)];
-    if (sum) atomicAdd(&P.hist[(size_t)it.seg * 1024 + e], sum);
+    for (uint32_t j = 0; j < L; ++j) sum += h[e * L + ((j + e) % L)];
+    if (sum) atomicAdd(&P.hist[(size_t)it.seg * D * R + e], sum);
   }
 }
 
+template <int RB>
 __device__ __forceinline__ void scan_item(const PlanDev& P, const Item& it, unsigned char* smem) {
+  constexpr uint32_t D = RB == 11 ? 3u : 4u, R = 1u << RB;
+  constexpr uint32_t PER = R >= kBlock ? R / kBlock : 1;  // bins per thread
   uint32_t* s_warp = reinterpret_cast<uint32_t*>(smem);
   const uint32_t tid = threadIdx.x;
-  for (int d = 0; d < 4; ++d) {
-    const uint32_t c = tid < 256 ? P.hist[(size_t)it.seg * 1024 + d * 256 + tid] : 0u;
-    const uint32_t x = block_exclusive_scan<kBlock>(c, s_warp);
-    if (tid < 256) P.bin_start[(size_t)it.seg * 1024 + d * 256 + tid] = x;
+  for (uint32_t d = 0; d < D; ++d) {
+    const uint32_t* hd = P.hist + (size_t)it.seg * D * R + d * R;
+    uint32_t c[PER];
+    uint32_t local = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < PER; ++i) {
+      const uint32_t b = tid * PER + i;
+      c[i] = b < R ? hd[b] : 0u;
+      local += c[i];
+    }
+    uint32_t run = block_exclusive_scan<kBlock>(local, s_warp);
+#pragma unroll
+    for (uint32_t i = 0; i < PER; ++i) {
+      const uint32_t b = tid * PER + i;
+      if (b < R) P.bin_start[(size_t)it.seg * D * R + d * R + b] = run;
+      run += c[i];
+    }
     __syncthreads();  // s_warp is reused by the next digit's scan
   }
 }
 
-template <int PASS_ITEMS>
+template <int PASS_ITEMS, int RB>
 __device__ __forceinline__ void pass_item(const PlanDev& P, const Item& it, unsigned char* smem, uint64_t* bar,
                                           uint32_t& parity) {
+  constexpr uint32_t D = RB == 11 ? 3u : 4u, R = 1u << RB;
   const LargeSeg L = P.large[it.seg];
   const bool even = (it.pass & 1u) == 0;
   TileJob<uint32_t, uint32_t> job;
@@ -98,14 +123,17 @@ __device__ __forceinline__ void pass_item(const PlanDev& P, const Item& it, unsi
   job.vout = nullptr;
   job.n = L.len;
   job.tile = it.idx;
-  job.shift = 8u * it.pass;
+  job.shift = RB * it.pass;
   job.tin = false;
   job.tout = false;
-  job.bin_start = P.bin_start + (size_t)it.seg * 1024 + it.pass * 256;
-  job.status = P.status + ((size_t)it.pass * P.total_tiles + L.tile_base) * 256;
+  job.bin_start = P.bin_start + (size_t)it.seg * D * R + it.pass * R;
+  job.status = P.status + ((size_t)it.pass * P.total_tiles + L.tile_base) * R;
   job.err = P.err;
   job.spin_limit = kSpinLimit;
-  onesweep_tile_multisplit<uint32_t, false, kBlock, PASS_ITEMS, uint32_t>(job, smem, bar, parity);
+  if constexpr (RB == 11)
+    onesweep_tile_wide<uint32_t, false, kBlock, PASS_ITEMS, 11, uint32_t>(job, smem, bar, parity);
+  else
+    onesweep_tile_multisplit<uint32_t, false, kBlock, PASS_ITEMS, uint32_t>(job, smem, bar, parity);
 }
 
 template <int SMALL_ITEMS>
@@ -131,7 +159,7 @@ __device__ __forceinline__ void small_item(const PlanDev& P, const Item& it, uns
   for (uint32_t i = threadIdx.x; i < len; i += kBlock) out[i] = s_keys[i];
 }
 
-template <int PASS_ITEMS, int SMALL_ITEMS>
+template <int PASS_ITEMS, int SMALL_ITEMS, int RB>
 __global__ void __launch_bounds__(kBlock, 2) segsort_kernel(const PlanDev P) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ Item s_item;
@@ -171,11 +199,11 @@ __global__ void __launch_bounds__(kBlock, 2) segsort_kernel(const PlanDev P) {
     if (it.kind == ITEM_SMALL)
       small_item<SMALL_ITEMS>(P, it, smem);
     else if (it.kind == ITEM_HIST)
-      hist_item(P, it, smem);
+      hist_item<RB>(P, it, smem);
     else if (it.kind == ITEM_SCAN)
-      scan_item(P, it, smem);
+      scan_item<RB>(P, it, smem);
     else
-      pass_item<PASS_ITEMS>(P, it, smem, s_bar, parity);
+      pass_item<PASS_ITEMS, RB>(P, it, smem, s_bar, parity);
     __syncthreads();
     if (it.kind != ITEM_SMALL && threadIdx.x == 0) {
       __threadfence();
@@ -186,33 +214,38 @@ __global__ void __launch_bounds__(kBlock, 2) segsort_kernel(const PlanDev P) {
 }
 
 // ---- host side ---------------------------------------------------------------
-template <int PI, int SI>
+template <int PI, int SI, int RB>
 constexpr size_t smem_bytes_for() {
-  using GP = Geometry<uint32_t, false, kBlock, PI>;
   using GS = Geometry<uint32_t, false, kBlock, SI>;
-  size_t b = GP::kBytes;
+  size_t b = RB == 11 ? WideGeometry<uint32_t, false, kBlock, PI, 11>::kBytes : Geometry<uint32_t, false, kBlock, PI>::kBytes;
   if (GS::kBytes > b) b = GS::kBytes;
-  if ((size_t)4 * 256 * kHistLanes * 4 > b) b = (size_t)4 * 256 * kHistLanes * 4;
+  const size_t hist = (size_t)(RB == 11 ? 3 : 4) * (1u << RB) * hist_lanes<RB>() * 4;
+  if (hist > b) b = hist;
   return b;
 }
 
 
-template <int PI, int SI>
+template <int PI, int SI, int RB>
 KernelChoice choice() {
-  return {segsort_kernel<PI, SI>, smem_bytes_for<PI, SI>(), (uint32_t)kBlock * PI, (uint32_t)kBlock * SI};
+  return {segsort_kernel<PI, SI, RB>, smem_bytes_for<PI, SI, RB>(), (uint32_t)kBlock * PI, (uint32_t)kBlock * SI};
 }
 
-bool pick_kernel(int tile_keys, int small_cutoff, KernelChoice* out) {
+template <int RB>
+bool pick_kernel_rb(int pi, int si, KernelChoice* out) {
+  if (pi == 8 && si == 4) *out = choice<8, 4, RB>();
+  if (pi == 8 && si == 8) *out = choice<8, 8, RB>();
+  if (pi == 8 && si == 16) *out = choice<8, 16, RB>();
+  if (pi == 16 && si == 4) *out = choice<16, 4, RB>();
+  if (pi == 16 && si == 8) *out = choice<16, 8, RB>();
+  if (pi == 16 && si == 16) *out = choice<16, 16, RB>();
+  return true;
+}
+
+bool pick_kernel(int tile_keys, int small_cutoff, int radix_bits, KernelChoice* out) {
   const int pi = tile_keys == 4096 ? 8 : tile_keys == 8192 ? 16 : 0;
   const int si = small_cutoff == 2048 ? 4 : small_cutoff == 4096 ? 8 : small_cutoff == 8192 ? 16 : 0;
   if (!pi || !si) return false;
-  if (pi == 8 && si == 4) *out = choice<8, 4>();
-  if (pi == 8 && si == 8) *out = choice<8, 8>();
-  if (pi == 8 && si == 16) *out = choice<8, 16>();
-  if (pi == 16 && si == 4) *out = choice<16, 4>();
-  if (pi == 16 && si == 8) *out = choice<16, 8>();
-  if (pi == 16 && si == 16) *out = choice<16, 16>();
-  return true;
+  return radix_bits == 11 ? pick_kernel_rb<11>(pi, si, out) : pick_kernel_rb<8>(pi, si, out);
 }
 
 // ---- host-side planning --------------------------------------------------------
@@ -226,9 +259,11 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
   if (c.small_cutoff == 0) c.small_cutoff = 4096;
   if (c.tile_keys == 0) c.tile_keys = 8192;
   if (c.digit_bits == 0) c.digit_bits = 8;
-  if (c.digit_bits != 8) return record_error(PA_ERR_ARG, "digit_bits must be 8 for the batched sort");
+  if (c.digit_bits != 8 && c.digit_bits != 11)
+    return record_error(PA_ERR_ARG, "digit_bits must be 8 or 11 for the batched sort");
+  if (c.digit_bits == 11) passes = 3;
   KernelChoice kc{};
-  if (!pick_kernel(c.tile_keys, c.small_cutoff, &kc))
+  if (!pick_kernel(c.tile_keys, c.small_cutoff, c.digit_bits, &kc))
     return record_error(PA_ERR_ARG, "tile_keys must be 4096 or 8192 and small_cutoff 2048, 4096 or 8192");
   const uint64_t* off = off_host;
   for (size_t i = 0; i < num_segments; ++i) {
@@ -239,6 +274,7 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
   hp->cfg = c;
   hp->kc = kc;
   hp->passes = (uint32_t)passes;
+  hp->radix_bits = (uint32_t)c.digit_bits;
   hp->off.assign(off, off + num_segments + 1);
   hp->items.clear();
   hp->large.clear();
@@ -297,12 +333,13 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
   hp->o_items = take(std::max<size_t>(items.size(), 1) * sizeof(Item));
   hp->o_off = take(hp->off.size() * 8);
   hp->o_large = take(nl * sizeof(LargeSeg));
-  hp->o_bins = take(nl * 1024 * 8);
+  const size_t per_seg = (size_t)seg_digits(hp->radix_bits) * seg_bins(hp->radix_bits);
+  hp->o_bins = take(nl * per_seg * 8);
   hp->o_err = take(256);
   hp->o_head = take(256);
   hp->o_done = take(nl * kStages * 4);
-  hp->o_hist = take(nl * 1024 * 4);
-  hp->o_status = take((size_t)kPasses * std::max<uint32_t>(total_tiles, 1) * 256 * 4);
+  hp->o_hist = take(nl * per_seg * 4);
+  hp->o_status = take((size_t)passes * std::max<uint32_t>(total_tiles, 1) * seg_bins(hp->radix_bits) * 4);
   hp->bytes = o;
   return PA_OK;
 }
@@ -323,6 +360,7 @@ PlanDev device_view(const HostPlan& hp, char* dev, uint32_t* keys, uint32_t* tmp
   d.status = reinterpret_cast<uint32_t*>(dev + hp.o_status);
   d.bin_start = reinterpret_cast<unsigned long long*>(dev + hp.o_bins);
   d.err = reinterpret_cast<uint32_t*>(dev + hp.o_err);
+  d.radix_bits = hp.radix_bits;
   return d;
 }
 
@@ -432,6 +470,9 @@ void destroy_graph(pa_segsort_plan* p) {
 
 int enqueue(pa_segsort_plan* p, cudaStream_t s) {
   PA_SEG_CUDA(launch_plan(p->hp, p->pd, p->dev, p->grid, s));
+  // an odd number of passes (11-bit digits: three) leaves every segment in tmp
+  if (p->hp.passes & 1u)
+    PA_SEG_CUDA(cudaMemcpyAsync(p->pd.keys, p->pd.tmp, (size_t)p->total_keys * 4, cudaMemcpyDeviceToDevice, s));
   return PA_OK;
 }
 

@@ -15,7 +15,7 @@ namespace pa {
 namespace seg {
 
 constexpr int kBlock = 512;
-constexpr int kPasses = 4;                  // uint32 keys, 8-bit digits
+constexpr int kPasses = 4;                  // uint32 keys, 8-bit digits (11-bit digits: 3 passes)
 constexpr uint32_t kHistChunk = 64 * 1024;  // keys per HIST item
 constexpr int kHistLanes = 8;               // lane-banked copies of each counter
 constexpr uint32_t kMaxSegmentKeys = (1u << 30) - 1;  // 32-bit look-back words
@@ -50,11 +50,16 @@ struct PlanDev {
   const LargeSeg* large;
   uint32_t* head;                  // zeroed per run
   uint32_t* done;                  // [large][kStages], zeroed per run
-  uint32_t* hist;                  // [large][4][256], zeroed per run
-  uint32_t* status;                // [kPasses][total_tiles][256], zeroed per run
-  unsigned long long* bin_start;   // [large][4][256]
+  uint32_t* hist;                  // [large][digits][bins], zeroed per run
+  uint32_t* status;                // [passes][total_tiles][bins], zeroed per run
+  unsigned long long* bin_start;   // [large][digits][bins]
   uint32_t* err;
+  uint32_t radix_bits;             // 8 (256 bins, 4 digits) or 11 (2048 bins, 3 digits)
 };
+
+// Digits of a 32-bit key and bins per digit for a digit width.
+__host__ __device__ inline uint32_t seg_digits(uint32_t radix_bits) { return radix_bits == 11 ? 3u : 4u; }
+__host__ __device__ inline uint32_t seg_bins(uint32_t radix_bits) { return 1u << radix_bits; }
 
 using KernelFn = void (*)(const PlanDev);
 
@@ -75,7 +80,9 @@ struct HostPlan {
   std::vector<LargeSeg> large;
   std::vector<uint64_t> off;
   uint32_t total_tiles = 0, num_small = 0, num_large = 0;
-  uint32_t passes = kPasses;  // digit passes of the large segments (3: every segment's top byte is constant)
+  uint32_t passes = kPasses;  // digit passes of the large segments (3: every segment's top byte is
+                              // constant; 3 with 11-bit digits)
+  uint32_t radix_bits = 8;
   size_t o_items = 0, o_off = 0, o_large = 0, o_bins = 0, o_err = 0, o_head = 0, o_done = 0, o_hist = 0,
          o_status = 0, bytes = 0;
 };
@@ -83,7 +90,8 @@ struct HostPlan {
 // Validates the offsets and plans the queue and the device block layout.
 // `passes` < 4 sorts large segments by their low `passes` bytes only (for
 // segments whose higher bytes are constant); results then end in tmp when
-// `passes` is odd (result_buffer).
+// `passes` is odd (result_buffer).  With cfg->digit_bits = 11 the plan runs
+// three 11-bit passes (and `passes` is ignored).
 int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segsort_config* cfg, HostPlan* hp,
                     int passes = kPasses);
 // Pointers of a device block laid out by `hp` (keys / tmp: the batch's keys).

@@ -40,11 +40,14 @@ def check(port, keys, out, off):
 
 @pytest.mark.parametrize("cutoff", [2048, 4096, 8192])
 @pytest.mark.parametrize("tile", [4096, 8192])
-def test_plan_every_config_matches_oracle(pa, port, torch_cuda, cutoff, tile):
+@pytest.mark.parametrize("bits", [8, 11])
+def test_plan_every_config_matches_oracle(pa, port, torch_cuda, cutoff, tile, bits):
+    """8-bit digits (four passes) and 11-bit digits (three passes of the
+    2048-bin tile, the result copied back from the scratch buffer)."""
     from parallelalgorithms_gb300.batched import SegmentedSortPlan, SegSortChoice
     torch = torch_cuda
     keys, off = make_segments(edge_sizes())
-    plan = SegmentedSortPlan(off, SegSortChoice(cutoff, tile), use_graph=True)
+    plan = SegmentedSortPlan(off, SegSortChoice(cutoff, tile, bits), use_graph=True)
     info = plan.info()
     assert info["small_segments"] > 0 and info["large_segments"] > 0
     d = torch.from_numpy(keys.view(np.int32).copy()).cuda()
