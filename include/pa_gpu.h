@@ -269,7 +269,10 @@ typedef struct pa_serve_config {
   int reserve_mib;          /* device memory (MiB, at most the budget) mapped into the
                                server's pool at creation, so that admissions do not wait
                                for the pool to map memory; 0 = map on demand */
-  int reserved[3];          /* must be zero */
+  int join_max_keys_log2;   /* only requests of at most 2^this keys share units with
+                               others; larger ones run alone: 0 = 20 */
+  int unit_max_keys_log2;   /* keys of one shared unit at most 2^this: 0 = 22 */
+  int reserved[1];          /* must be zero */
 } pa_serve_config;
 typedef struct pa_server pa_server;
 

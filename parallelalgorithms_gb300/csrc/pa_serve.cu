@@ -470,6 +470,11 @@ int pa_server_create(const pa_serve_config* cfg, pa_server** out) {
   if (c.hbm_budget_bytes) sc.budget_bytes = c.hbm_budget_bytes;
   if (c.max_inflight > 0) sc.max_inflight = c.max_inflight;
   if (c.max_batch_requests > 0) sc.max_batch_requests = c.max_batch_requests;
+  if (c.join_max_keys_log2 < 0 || c.join_max_keys_log2 > 40 || c.unit_max_keys_log2 < 0 ||
+      c.unit_max_keys_log2 > 40)
+    return record_error(PA_ERR_ARG, "pa_serve_config: key limits are powers of two up to 2^40");
+  if (c.join_max_keys_log2 > 0) sc.max_join_keys = (size_t)1 << c.join_max_keys_log2;
+  if (c.unit_max_keys_log2 > 0) sc.max_batch_keys = sc.max_group_keys = (size_t)1 << c.unit_max_keys_log2;
   sc.coalesce = c.no_coalesce == 0;
   const int lanes = c.num_streams > 0 ? c.num_streams : 4;
   auto* s = new pa_server();

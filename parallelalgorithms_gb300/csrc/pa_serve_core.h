@@ -57,10 +57,13 @@ struct Config {
   size_t budget_bytes = (size_t)64 << 30;
   int max_inflight = 4;             // units on the device at once
   int max_batch_requests = 256;     // requests coalesced into one launch
-  size_t max_batch_keys = (size_t)1 << 28;   // keys of a segmented (32-bit sort) unit
-  size_t max_group_keys = (size_t)1 << 24;   // keys of any other shared unit: its requests run
-                                             // one after another, so large ones stay alone and
-                                             // overlap on the other streams
+  // Only requests of at most max_join_keys keys share units: for them the
+  // fixed cost of a unit (allocation, copies, launches, event) is a large
+  // part of the time.  Larger requests run alone, so that their copies and
+  // kernels overlap those of the units on the other streams.
+  size_t max_join_keys = (size_t)1 << 20;
+  size_t max_batch_keys = (size_t)1 << 22;   // keys of a segmented (32-bit sort) unit
+  size_t max_group_keys = (size_t)1 << 22;   // keys of any other shared unit
   size_t window = 1024;             // waiting requests scanned for coalescing
   bool coalesce = true;
 };
@@ -191,13 +194,13 @@ class Scheduler {
     Request* head = waiting_.front();
     u.reqs.push_back(head);
     const size_t limit = segmented(head) ? cfg_.max_batch_keys : cfg_.max_group_keys;
-    if (cfg_.coalesce && head->n < limit) {
+    if (cfg_.coalesce && head->n <= cfg_.max_join_keys && head->n < limit) {
       size_t keys = head->n;
       size_t scanned = 0;
       for (auto it = std::next(waiting_.begin()); it != waiting_.end() && scanned < cfg_.window; ++it, ++scanned) {
         if ((int)u.reqs.size() >= cfg_.max_batch_requests) break;
         if (!same_kind(head, *it)) continue;
-        if (keys + (*it)->n > limit) continue;
+        if ((*it)->n > cfg_.max_join_keys || keys + (*it)->n > limit) continue;
         keys += (*it)->n;
         u.reqs.push_back(*it);
       }

@@ -36,7 +36,9 @@ class PaRequest(ctypes.Structure):
 class ServeConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_inflight", ctypes.c_int),
                 ("max_batch_requests", ctypes.c_int), ("no_coalesce", ctypes.c_int),
-                ("num_streams", ctypes.c_int), ("reserve_mib", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("num_streams", ctypes.c_int), ("reserve_mib", ctypes.c_int),
+                ("join_max_keys_log2", ctypes.c_int), ("unit_max_keys_log2", ctypes.c_int),
+                ("reserved", ctypes.c_int * 1)]
 
 
 @dataclass
@@ -73,10 +75,12 @@ class Request:
 
 class Server:
     def __init__(self, budget_bytes: int = 64 << 30, max_inflight: int = 4, max_batch_requests: int = 256,
-                 coalesce: bool = True, num_streams: int = 4, reserve_bytes: int = 0):
+                 coalesce: bool = True, num_streams: int = 4, reserve_bytes: int = 0,
+                 join_max_keys_log2: int = 0, unit_max_keys_log2: int = 0):
         cfg = ServeConfig(hbm_budget_bytes=budget_bytes, max_inflight=max_inflight,
                           max_batch_requests=max_batch_requests, no_coalesce=0 if coalesce else 1,
-                          num_streams=num_streams, reserve_mib=(reserve_bytes + (1 << 20) - 1) >> 20)
+                          num_streams=num_streams, reserve_mib=(reserve_bytes + (1 << 20) - 1) >> 20,
+                          join_max_keys_log2=join_max_keys_log2, unit_max_keys_log2=unit_max_keys_log2)
         h = ctypes.c_void_p()
         call("pa_server_create", ctypes.byref(cfg), ctypes.byref(h))
         self._h = h

@@ -119,6 +119,25 @@ int main() {
     CHECK(b.units[1].size() == 1 && b.units[1][0] == &rs[1]);
     CHECK(b.units[2].size() == 1 && b.units[2][0] == &rs[3]);
   }
+  // 1c. requests above max_join_keys run alone, as the head or among waiting ones
+  {
+    FakeBackend b;
+    Config c;
+    c.max_inflight = 8;
+    c.max_join_keys = 40;
+    Scheduler<FakeBackend> s(b, c);
+    std::vector<Request> rs;
+    rs.push_back(make(OP_SORT, 4, 50));  // head above the join limit: alone
+    rs.push_back(make(OP_SORT, 4, 10));
+    rs.push_back(make(OP_SORT, 4, 41));  // above the limit: skipped by the group
+    rs.push_back(make(OP_SORT, 4, 40));  // at the limit: joins
+    for (auto& r : rs) s.submit(&r);
+    run_to_idle(s);
+    CHECK(b.units.size() == 3);
+    CHECK(b.units[0].size() == 1 && b.units[0][0] == &rs[0]);
+    CHECK(b.units[1].size() == 2 && b.units[1][0] == &rs[1] && b.units[1][1] == &rs[3]);
+    CHECK(b.units[2].size() == 1 && b.units[2][0] == &rs[2]);
+  }
   // 2. coalescing off: every request alone
   {
     FakeBackend b;
