@@ -123,6 +123,20 @@ int pa_sort_timed(int key_kind, void* keys, void* tmp, uint32_t* vals, uint32_t*
  * Synchronous; returns PA_ERR_ARG for host buffers or n above the limit. */
 int pa_sort_u32_noalloc(uint32_t* keys, uint32_t* tmp, size_t n, const pa_opts* opts);
 
+/* In-place sort of 32-bit keys with bounded device scratch: replaces
+ * parallel_hybrid_inplace_msd_radix_sort(a, a_size) (RadixSortMsdParallel.h:291),
+ * whose point is to sort without a second array of n keys.  Besides the keys
+ * (for host keys: their device copy) the call holds scratch_keys keys of
+ * device scratch (0 = 2^24 = 64 MiB, at least 2^16) and about scratch_keys
+ * / 2 + 8 MiB bytes of tables, whatever n is.  Up to scratch_keys keys it is
+ * the LSD sort with the scratch as its second buffer; above, ranges are
+ * partitioned in place by a digit (top digit first) through the scratch and
+ * buckets of at most scratch_keys keys are sorted in groups by the batched
+ * segmented sort.  Same sorted array as pa_sort_u32.  For keys above 2^24
+ * the call waits for the device once per partitioned range (it reads the
+ * range's digit counts back to plan the buckets). */
+int pa_sort_u32_inplace(uint32_t* keys, size_t n, size_t scratch_keys, const pa_opts* opts);
+
 /* ---- digit histograms ----------------------------------------------------
  * pa_hist_byte_components_u32: out[d * 256 + b] = number of keys in a[0, n)
  *   whose byte d (d = 0..3, least significant first) equals b, from one read.

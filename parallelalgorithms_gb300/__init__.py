@@ -439,10 +439,12 @@ def parallel_linear_in_place_preventative_adaptive_sort(src, src_size: int | Non
     sort(src, n=src_size)
 
 
-def parallel_hybrid_inplace_msd_radix_sort(a, a_size: int | None = None) -> None:
-    """RadixSortMsdParallel.h:291: sorts a[0, a_size) in place (for keys
-    alone the unstable MSD sort and this LSD sort give the same array)."""
+def parallel_hybrid_inplace_msd_radix_sort(a, a_size: int | None = None, scratch_keys: int = 0) -> None:
+    """RadixSortMsdParallel.h:291: sorts a[0, a_size) in place holding a
+    bounded device scratch (scratch_keys keys, 0 = 2^24) instead of a second
+    array of a_size keys (pa_sort_u32_inplace).  For keys alone the unstable
+    MSD sort gives the same array as any sort."""
     _require_u32(a)
     n = _info(a)[1] if a_size is None else a_size
     if n >= 2:
-        sort(a, n=n)
+        call("pa_sort_u32_inplace", _ptr(a), n, scratch_keys, _opts(a))

@@ -34,6 +34,7 @@ _O = ctypes.POINTER(PaOpts)
 # name -> argtypes; every entry point returns int (pa_status)
 SIGNATURES: dict[str, list] = {
     "pa_sort_u32": [_P, _P, _SZ, _O],
+    "pa_sort_u32_inplace": [_P, _SZ, _SZ, _O],
     "pa_sort_u64": [_P, _P, _SZ, _O],
     "pa_sort_f32": [_P, _P, _SZ, _O],
     "pa_sort_kv_u32": [_P, _P, _P, _P, _SZ, _O],

@@ -23,7 +23,8 @@ LIB = PKG / "libpa_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["pa_capi.cu", "pa_histogram.cu", "pa_onesweep.cu", "pa_sum.cu", "pa_select.cu", "pa_pipeline.cu",
-                "pa_segmented.cu", "pa_noalloc.cu", "pa_serve.cu", "pa_partition.cu"]
+                "pa_segmented.cu", "pa_noalloc.cu", "pa_serve.cu", "pa_partition.cu",
+                "pa_inplace.cu"]
 HOST_SOURCES = ["pa_workloads.cpp"]
 
 

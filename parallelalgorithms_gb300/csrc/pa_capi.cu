@@ -553,6 +553,163 @@ int sort_impl(void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t 
 }
 
 // ---------------------------------------------------------------------------
+// In-place sort with bounded scratch
+// ---------------------------------------------------------------------------
+// An MSD sort of 32-bit keys that holds, besides the keys, a scratch of S
+// keys (and small tables) whatever n is.  Up to S keys: the LSD sort with
+// the scratch as its second buffer.  Above: a range is partitioned in place
+// on its top digit (launch_inplace_partition, rounds through the scratch
+// halves); buckets of at most S keys are sorted in groups of consecutive
+// buckets (at most S keys a group) on their lower digits by the batched
+// segmented sort, with the scratch as its second buffer; larger buckets are
+// partitioned again on the next digit.  A range whose keys all share the
+// digit is not moved.
+constexpr size_t kInplaceDefaultScratch = (size_t)1 << 24;  // keys
+constexpr size_t kInplaceMinScratch = (size_t)1 << 16;
+
+int inplace_levels(Workspace* ws, cudaStream_t stream, uint32_t* a, size_t n, size_t S, uint32_t* buf,
+                   InplaceState* st, void* status, unsigned long long* hist, char* plan_dev, size_t plan_cap,
+                   char* sort_base) {
+  struct Range {
+    size_t lo, len;
+    uint32_t shift;
+  };
+  std::vector<Range> todo{{0, n, 24}};
+  std::vector<unsigned long long> h(256);
+  const size_t half = S / 2;
+  while (!todo.empty()) {
+    const Range rg = todo.back();
+    todo.pop_back();
+    PA_CUDA(cudaMemsetAsync(hist, 0, 256 * sizeof(unsigned long long), stream));
+    PA_CUDA(launch_digit_counts(a + rg.lo, rg.len, 4, 1, 8, rg.shift, 0, false, hist, stream));
+    PA_CUDA(cudaMemcpyAsync(h.data(), hist, 256 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
+    PA_CUDA(cudaStreamSynchronize(stream));
+    int nonempty = 0;
+    for (unsigned long long c : h) nonempty += c ? 1 : 0;
+    if (nonempty <= 1) {  // every key has this digit: nothing moves
+      if (rg.shift > 0) todo.push_back({rg.lo, rg.len, rg.shift - 8});
+      continue;
+    }
+    PA_CUDA(launch_inplace_partition(a + rg.lo, rg.len, rg.shift, hist, buf, buf + half, half, st, status, ws->err,
+                                     stream));
+    if (rg.shift == 0) continue;  // the buckets of the lowest digit hold equal keys
+    // groups of consecutive buckets of at most S keys, larger buckets to the next level
+    const int passes = (int)(rg.shift / 8);  // digits below this one
+    struct Group {
+      size_t lo;
+      std::vector<uint64_t> off;
+    };
+    std::vector<Group> groups;
+    size_t at = rg.lo;
+    bool open = false;
+    for (int b = 0; b < 256; ++b) {
+      const size_t c = (size_t)h[b];
+      if (c == 0) continue;
+      if (c > S) {
+        todo.push_back({at, c, rg.shift - 8});
+        open = false;
+      } else {
+        if (!open || groups.back().off.back() + c > S) {
+          groups.push_back({at, {0}});
+          open = true;
+        }
+        groups.back().off.push_back(groups.back().off.back() + c);
+      }
+      at += c;
+    }
+    std::vector<seg::HostPlan> plans(groups.size());
+    std::vector<bool> planned(groups.size(), false);
+    std::vector<size_t> image_off(groups.size() + 1, 0);
+    for (size_t g = 0; g < groups.size(); ++g) {
+      size_t bytes = 0;
+      if (groups[g].off.back() > 1) {
+        pa_segsort_config cfg{};
+        cfg.small_cutoff = 4096;
+        cfg.tile_keys = 8192;
+        planned[g] = seg::build_host_plan(groups[g].off.data(), groups[g].off.size() - 1, &cfg, &plans[g],
+                                          passes) == PA_OK &&
+                     plans[g].bytes <= plan_cap;
+        if (planned[g]) bytes = seg::plan_image_bytes(plans[g]);
+      }
+      image_off[g + 1] = image_off[g] + (bytes + 255) / 256 * 256;
+    }
+    char* images = static_cast<char*>(pipe_pinned(ws, image_off.back() + 256));
+    if (!images) return set_error(PA_ERR_OOM, "page-locked staging for the in-place sort's plans");
+    for (size_t g = 0; g < groups.size(); ++g) {
+      uint32_t* ga = a + groups[g].lo;
+      const size_t glen = (size_t)groups[g].off.back();
+      if (glen < 2) continue;
+      if (planned[g]) {
+        seg::HostPlan& hp = plans[g];
+        PA_CUDA(seg::upload_plan(hp, plan_dev, stream, images + image_off[g]));
+        seg::PlanDev pd = seg::device_view(hp, plan_dev, ga, buf);
+        pd.err = ws->err;
+        PA_CUDA(seg::launch_plan(hp, pd, plan_dev, seg::plan_grid(hp), stream));
+        if (seg::result_buffer(pd) != ga)
+          PA_CUDA(cudaMemcpyAsync(ga, seg::result_buffer(pd), glen * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                                  stream));
+      } else {  // the group as one array: its buckets are already in order
+        SortScratch sc{};
+        sort_scratch_layout(sort_base, glen, 4, false, &sc);
+        PA_CUDA(enqueue_sort(sc, ga, buf, nullptr, nullptr, glen, 4, false, ws->err, stream));
+      }
+    }
+  }
+  return PA_OK;
+}
+
+int inplace_impl(uint32_t* keys, size_t n, size_t scratch_keys, const pa_opts* opts) {
+  if (int rc = check_opts(opts)) return rc;
+  if (opts && opts->digit_bits == 11) return set_error(PA_ERR_ARG, "the in-place sort takes 8-bit digits only");
+  if (n == 0) return PA_OK;
+  if (!keys) return set_error(PA_ERR_ARG, "keys is NULL");
+  if (n == 1) return PA_OK;
+  if (int rc = device_ready()) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t stream = stream_of(opts);
+  Workspace* ws = nullptr;
+  if (int rc = get_workspace(stream, &ws)) return rc;
+  size_t S = scratch_keys ? std::max(scratch_keys, kInplaceMinScratch) : kInplaceDefaultScratch;
+  S &= ~(size_t)1;
+  const bool keys_dev = is_device_ptr(keys);
+  const size_t sort_keys = std::min(n, S);
+  const size_t plan_cap = S / 2 + ((size_t)8 << 20);
+  uint32_t *d_keys = nullptr, *buf = nullptr;
+  InplaceState* st = nullptr;
+  unsigned long long* hist = nullptr;
+  char *plan_dev = nullptr, *sort_base = nullptr, *status = nullptr;
+  auto layout = [&](Carve& c) {
+    d_keys = keys_dev ? keys : c.take<uint32_t>(n);
+    buf = c.take<uint32_t>(sort_keys);
+    sort_base = c.take<char>(sort_scratch_bytes(sort_keys, 4, false));
+    if (n > S) {
+      st = c.take<InplaceState>(1);
+      hist = c.take<unsigned long long>(256);
+      plan_dev = c.take<char>(plan_cap);
+      status = c.take<char>(inplace_status_bytes(n, S / 2));
+    }
+  };
+  Carve measure{nullptr};
+  layout(measure);
+  if (int rc = ensure_dev(ws, stream, measure.off)) return rc;
+  Carve real{ws->dev};
+  layout(real);
+  if (!keys_dev) PA_CUDA(cudaMemcpyAsync(d_keys, keys, n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+  if (n <= S) {
+    SortScratch sc{};
+    sort_scratch_layout(sort_base, n, 4, false, &sc);
+    PA_CUDA(enqueue_sort(sc, d_keys, buf, nullptr, nullptr, n, 4, false, ws->err, stream));
+  } else if (int rc = inplace_levels(ws, stream, d_keys, n, S, buf, st, status, hist, plan_dev, plan_cap,
+                                     sort_base)) {
+    cudaStreamSynchronize(stream);
+    cudaGetLastError();
+    return rc;
+  }
+  if (!keys_dev) PA_CUDA(cudaMemcpyAsync(keys, d_keys, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+  return finish(ws, stream, opts && opts->async_device && keys_dev);
+}
+
+// ---------------------------------------------------------------------------
 // Histograms
 // ---------------------------------------------------------------------------
 // One histogram call: `rows` x 256 counts of the digits selected by
@@ -843,6 +1000,9 @@ int pa_release_workspaces(void) {
 
 int pa_sort_u32(uint32_t* keys, uint32_t* tmp, size_t n, const pa_opts* opts) {
   return sort_impl(keys, tmp, nullptr, nullptr, n, 4, false, opts);
+}
+int pa_sort_u32_inplace(uint32_t* keys, size_t n, size_t scratch_keys, const pa_opts* opts) {
+  return inplace_impl(keys, n, scratch_keys, opts);
 }
 int pa_sort_timed(int key_kind, void* keys, void* tmp, uint32_t* vals, uint32_t* tmp_vals, size_t n,
                   float* phase_ms, int phase_cap, const pa_opts* opts) {

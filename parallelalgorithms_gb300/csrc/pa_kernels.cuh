@@ -118,6 +118,11 @@ struct OnesweepArgs {
   uint32_t spin_limit = 0;  // look-back polls before a tile gives up; 0 = kSpinLimit
   size_t max_ctas = 0;      // CTAs launched; 0 = one per tile (only the wait-expiry self-test sets it)
   int radix_bits = 8;       // digit width: 8 (256 bins) or 11 (2048 bins)
+  // 8-bit passes only: the keys to move counted on the device (at most n;
+  // the grid is sized for n, tiles past the count exit), and a bound on the
+  // output positions when the output is not an n-key array (0: n)
+  const unsigned long long* n_dev = nullptr;
+  size_t out_n = 0;
 };
 
 // Tile geometry chosen for (key_bytes, has_vals, radix_bits); the workspace
@@ -223,6 +228,31 @@ constexpr int kPartitionMaxPivots = 7;
 size_t partition_scratch_words(size_t n, int m);
 cudaError_t launch_partition(const uint32_t* in, uint32_t* out, size_t n, const uint32_t* pivots, int m,
                              unsigned long long* scratch, cudaStream_t stream);
+
+// ---- in-place partition by one digit (pa_inplace.cu) -----------------------
+// Per-bucket cursors and the current round's plan of an in-place partition.
+struct InplaceState {
+  unsigned long long w[256];       // write cursor
+  unsigned long long r[256];       // end of the unread part
+  unsigned long long cursor[256];  // the round's scatter cursors
+  unsigned long long cnt[2][256];  // digit counts of the keys in hand in each half
+  unsigned long long run_src[256], run_len[256], run_dst[256];  // the runs of the next copy
+  unsigned long long hand[2];      // keys in hand in each half
+  unsigned long long total;        // keys scattered by the round
+  unsigned long long run_base, run_keys;  // the copy's destination range
+  SortCtrl ctrl;                   // the scatter pass's control (one pass, keys_a -> keys_b)
+  uint32_t ticket;                 // the scatter pass's tile ticket
+};
+// keys[0, n) arranged in place in the buckets of the digit (key >> shift) &
+// 255 (bucket order; order inside a bucket unspecified), given hist, the
+// range's 256 digit counts (device).  c0, c1: scratch halves of `half` keys
+// each; st: device state; status: inplace_status_bytes(n, half) bytes of
+// look-back words.  Enqueues ceil(n / half) + 1 rounds of five launches;
+// nothing is read back.
+size_t inplace_status_bytes(size_t n, size_t half);
+cudaError_t launch_inplace_partition(uint32_t* keys, size_t n, uint32_t shift, const unsigned long long* hist,
+                                     uint32_t* c0, uint32_t* c1, size_t half, InplaceState* st, void* status,
+                                     uint32_t* err, cudaStream_t stream);
 
 // ---- select (pa_select.cu) -------------------------------------------------
 struct SelectState;

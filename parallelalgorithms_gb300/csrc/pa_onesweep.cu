@@ -60,8 +60,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
   }
   __syncthreads();
   const uint32_t tile = *s_tile_id;
-  if ((size_t)tile >= (args.n + TILE - 1) / TILE) {  // a ticket counter that was not reset
-    if (threadIdx.x == 0) raise_error(args.err, DEVERR_BAD_STATE);
+  // keys to move: args.n, or fewer counted on the device (tiles past them exit)
+  const size_t n = args.n_dev ? min((size_t)*args.n_dev, args.n) : args.n;
+  if ((size_t)tile >= (n + TILE - 1) / TILE) {
+    if (!args.n_dev && threadIdx.x == 0) raise_error(args.err, DEVERR_BAD_STATE);  // a ticket counter not reset
     return;
   }
   TileJob<K, S> job;
@@ -69,7 +71,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
   job.out = static_cast<K*>(pc.src_is_tmp ? args.keys_a : args.keys_b);
   job.vin = pc.src_is_tmp ? args.vals_b : args.vals_a;
   job.vout = pc.src_is_tmp ? args.vals_a : args.vals_b;
-  job.n = args.n;
+  job.n = n;
+  job.out_n = args.out_n ? args.out_n : n;
   job.tile = tile;
   job.shift = args.shift;
   job.tin = args.is_float && pc.transform_in;
@@ -112,6 +115,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_wide_kernel(const Oneswe
   job.vin = pc.src_is_tmp ? args.vals_b : args.vals_a;
   job.vout = pc.src_is_tmp ? args.vals_a : args.vals_b;
   job.n = args.n;
+  job.out_n = args.n;
   job.tile = tile;
   job.shift = args.shift;
   job.tin = args.is_float && pc.transform_in;
@@ -273,7 +277,8 @@ cudaError_t launch_g(const OnesweepArgs& a, cudaStream_t stream) {
 
 template <typename K, bool HAS_VALS, int BLOCK, int ITEMS, int MINB>
 cudaError_t launch_s(const OnesweepArgs& a, cudaStream_t stream) {
-  if (a.n < (1ull << 30)) return launch_g<K, HAS_VALS, BLOCK, ITEMS, MINB, uint32_t>(a, stream);
+  if (a.n < (1ull << 30) && a.out_n < (1ull << 30))
+    return launch_g<K, HAS_VALS, BLOCK, ITEMS, MINB, uint32_t>(a, stream);
   return launch_g<K, HAS_VALS, BLOCK, ITEMS, MINB, unsigned long long>(a, stream);
 }
 

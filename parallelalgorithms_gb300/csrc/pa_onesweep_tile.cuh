@@ -200,6 +200,7 @@ struct TileJob {
   const uint32_t* vin;
   uint32_t* vout;
   size_t n;
+  size_t out_n;  // output positions are below this (n, or the output array's length)
   uint32_t tile;
   uint32_t shift;
   bool tin;
@@ -389,7 +390,7 @@ __device__ __forceinline__ void onesweep_tile(const TileJob<K, S>& job, unsigned
     if (tma_pending) mbar_wait_bounded(s_bar, parity ^ 1u, job.err);
     return;
   }
-  const S n_out = (S)job.n;
+  const S n_out = (S)job.out_n;
   auto scatter = [&](auto transform) {
     if (full) {
 #pragma unroll 4
@@ -731,7 +732,7 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
     if (tma_pending) mbar_wait_bounded(s_bar, parity ^ 1u, job.err);
     return;
   }
-  const S n_out = (S)job.n;
+  const S n_out = (S)job.out_n;
   auto scatter = [&](auto transform) {
     if (full) {
 #pragma unroll 4
@@ -1017,7 +1018,7 @@ __device__ __forceinline__ void onesweep_tile_wide(const TileJob<K, S>& job, uns
     if (tma_pending) mbar_wait_bounded(s_bar, parity ^ 1u, job.err);
     return;
   }
-  const S n_out = (S)job.n;
+  const S n_out = (S)job.out_n;
   const bool full = tile_n == (uint32_t)TILE;
   auto scatter = [&](auto toutc) {
     constexpr bool TOUT = decltype(toutc)::value;

@@ -122,6 +122,7 @@ __device__ __forceinline__ void pass_item(const PlanDev& P, const Item& it, unsi
   job.vin = nullptr;
   job.vout = nullptr;
   job.n = L.len;
+  job.out_n = L.len;
   job.tile = it.idx;
   job.shift = RB * it.pass;
   job.tin = false;

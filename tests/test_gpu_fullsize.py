@@ -51,6 +51,10 @@ def test_u32_100m_against_the_compiled_reference(pa, ref, torch_cuda, inputs, di
     d = torch_cuda.from_numpy(a.view(np.int32)).cuda()
     pa.SortRadixPar(d, torch_cuda.empty_like(d), N)
     np.testing.assert_array_equal(d.cpu().numpy().view(np.uint32), want)
+    # the in-place MSD sort (bounded scratch: partition rounds, then bucket groups)
+    d.copy_(torch_cuda.from_numpy(a.view(np.int32)))
+    pa.parallel_hybrid_inplace_msd_radix_sort(d)
+    np.testing.assert_array_equal(d.cpu().numpy().view(np.uint32), want)
     del d
     np.testing.assert_array_equal(pa.HistogramOneByteComponentParallel(a, 0, N - 1, 0),
                                   ref.hist_one_byte(a, 0, N - 1, 0))
