@@ -20,7 +20,9 @@ Printed as one JSON line (rank 0):
               stand-in thread pool) on this host's cores, same input
   extras      presorted / constant sorts, 64-bit key+payload and float32
               sorts, low-digit histogram, select k = n/2 and 64-bit sum at
-              100M, each with its own bytes-moved roofline fraction
+              100M, each with its own bytes-moved roofline fraction; byte
+              counting sort, PartitionRadix, the bounded-scratch in-place
+              sort, the batched segmented sort and the serving stream
 
 --impl reference times the reference's CPU SortRadixPar on the same
 workload (rank 0 only under torchrun; other ranks exit without work).
@@ -69,7 +71,7 @@ def parse_args():
     # seeded input and prints no JSON line (the commands in profiles/ use it)
     p.add_argument("--profile-op", default=None,
                    choices=["sort_u32", "sort_u32_host", "sort_u64", "sort_kv_u64", "sort_f32", "hist_u32",
-                            "select_u32", "sum_u32"])
+                            "select_u32", "sum_u32", "sort_u32_inplace", "partition_u32"])
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--dist", default="uniform", choices=["uniform", "presorted", "constant"])
     return p.parse_args()
@@ -82,7 +84,8 @@ def profile_op(a) -> None:
     device-resident.  Per sort: the workspace memset, one digit histogram,
     one scan, one onesweep launch per key byte, one final copy.
     `sort_u32_host` sorts a page-locked host copy through the C ABI instead
-    (the pipelined host-buffer path)."""
+    (the pipelined host-buffer path); `sort_u32_inplace` is the bounded-scratch
+    in-place sort, `partition_u32` PartitionRadix around k = n/2 and n - 21."""
     import torch
 
     from parallelalgorithms_gb300 import _native, build, workloads
@@ -132,6 +135,11 @@ def profile_op(a) -> None:
             _native.call("pa_select_u32", P(k.data_ptr()), n, n // 2, P(out.data_ptr()), o)
         elif op == "sum_u32":
             _native.call("pa_sum_u32", P(k.data_ptr()), n, P(out.data_ptr()), o)
+        elif op == "sort_u32_inplace":
+            _native.call("pa_sort_u32_inplace", P(k.data_ptr()), n, 0, o)
+        elif op == "partition_u32":
+            ks = np.array([n // 2, n - 21], np.uint64)
+            _native.call("pa_partition_radix_u32", P(k.data_ptr()), n, P(ks.ctypes.data), ks.size, o)
     torch.cuda.synchronize()
     print(f"profile driver done: op={op} n={n} reps={a.reps}")
 
@@ -606,6 +614,7 @@ def serving_extra(count: int = 120) -> dict:
             serving.run_served(srv, specs, bufs, None)  # warm the server's pinned staging blocks
             reqs = serving.run_served(srv, specs, bufs, None)
             sat.append((span_of(reqs), reqs, srv.stats()))
+    in_order = [x[0] for x in sat]
     sat.sort(key=lambda x: x[0])
     span, reqs, sat_stats = sat[len(sat) // 2]
     spans = [x[0] for x in sat]
@@ -613,7 +622,8 @@ def serving_extra(count: int = 120) -> dict:
                                 **serving.latency_stats(reqs), "latency": "submit to completion (includes queueing)",
                                 "speedup_vs_plain_per_request": plain_s / span,
                                 "speedup_all_servers": sorted(plain_s / x for x in spans),
-                                "makespans_s": spans, "servers": len(sat),
+                                "makespans_s": spans, "makespans_s_in_creation_order": in_order,
+                                "servers": len(sat),
                                 "server_stats": sat_stats,
                                 "shared_unit_requests_share": sat_stats["coalesced_requests"] / max(1, sat_stats["completed"])}
     with serving.Server(**kw) as srv:
@@ -743,7 +753,21 @@ def run_extras(pa, lib, _native, workloads, n, stream, peak) -> dict:
     out["partition_radix_2k_uniform"] = {"ms": ms, "keys_per_s": n / (ms / 1e3),
                                          "how": "one select per k, then one bucket pass (count, scan, write) and a copy back",
                                          "bytes_per_key": 4 * 2 + 4 + 8 + 8}
-    del d, pw
+    # in-place MSD sort (RadixSortMsdParallel.h:291) holding the default
+    # bounded scratch (2^24 keys) instead of a second array of n keys
+    ms = _time_device(lambda: _native.call("pa_sort_u32_inplace", P(pw.data_ptr()), n, 0, o), 5, stream,
+                      lambda: pw.copy_(d))
+    ref_sorted = d.clone()
+    _native.call("pa_sort_u32", P(ref_sorted.data_ptr()), None, n, o)
+    torch.cuda.synchronize()
+    out["sort_u32_inplace_bounded_scratch"] = {
+        "ms": ms, "keys_per_s": n / (ms / 1e3), "scratch_bytes": 4 << 24, "plain_sort_second_buffer_bytes": 4 * n,
+        "same_as_plain_sort": bool(torch.equal(pw, ref_sorted)),
+        "how": "top digit partitioned in place in rounds through two 2^23-key scratch halves, bucket groups "
+               "sorted by the batched segmented sort on the low three digits; includes the host's wait for "
+               "the top digit's counts",
+        "bytes_per_key": 4 + 16 + 4 + 3 * 8 + 8}
+    del d, pw, ref_sorted
     out["batched_segmented_sort_4096_arrays"] = batched_extra(lib, _native, workloads, stream, peak)
     out["serving_c5"] = serving_extra()
     return out
