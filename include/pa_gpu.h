@@ -297,8 +297,10 @@ int pa_server_submit(pa_server* server, pa_request* req);
 int pa_server_wait(pa_server* server, pa_request* req);
 /* Blocks until every submitted request has completed. */
 int pa_server_drain(pa_server* server);
-/* out[0..6] = submitted, completed, rejected (over budget), units launched,
- * batched units, requests served in batches, peak device bytes held. */
+/* out[0..8] = submitted, completed, rejected (over budget), units launched,
+ * batched units, requests served in batches, peak device bytes held, and the
+ * scheduler thread's microseconds spent enqueueing units and completing them
+ * (count bounds how many are written). */
 int pa_server_stats(pa_server* server, uint64_t* out, int count);
 int pa_server_destroy(pa_server* server);
 

@@ -71,6 +71,7 @@ struct Config {
 struct Stats {
   size_t submitted = 0, completed = 0, rejected = 0, units = 0, batched_units = 0, coalesced_requests = 0;
   size_t peak_bytes = 0;
+  double launch_s = 0, finish_s = 0;  // scheduler-thread time spent enqueueing units / completing them
 };
 
 template <class Backend>
@@ -103,7 +104,9 @@ class Scheduler {
     }
     for (auto it = inflight_.begin(); it != inflight_.end();) {
       if (b_.finished(*it)) {
+        const double f0 = b_.now();
         b_.finish(*it);
+        stats_.finish_s += b_.now() - f0;
         in_use_ -= it->bytes;
         const double t = b_.now();
         for (Request* r : it->reqs) {
@@ -158,7 +161,9 @@ class Scheduler {
         stats_.coalesced_requests += u.reqs.size();
       }
       inflight_.push_back(std::move(u));
+      const double l0 = b_.now();
       b_.launch(inflight_.back());
+      stats_.launch_s += b_.now() - l0;
       progress = true;
     }
     return progress;

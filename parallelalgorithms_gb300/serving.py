@@ -95,9 +95,10 @@ class Server:
         call("pa_server_drain", self._h)
 
     def stats(self) -> dict:
-        out = (ctypes.c_uint64 * 7)()
-        call("pa_server_stats", self._h, out, 7)
-        keys = ["submitted", "completed", "rejected", "units", "batched_units", "coalesced_requests", "peak_bytes"]
+        out = (ctypes.c_uint64 * 9)()
+        call("pa_server_stats", self._h, out, 9)
+        keys = ["submitted", "completed", "rejected", "units", "batched_units", "coalesced_requests", "peak_bytes",
+                "launch_us", "finish_us"]
         return dict(zip(keys, list(out)))
 
     def close(self) -> None:
