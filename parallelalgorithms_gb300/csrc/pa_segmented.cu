@@ -11,9 +11,12 @@
 //   HIST  one chunk of a large segment: its four byte-digit counts, added
 //         into the segment's histogram;
 //   SCAN  one large segment: bin starts of its four digits;
-//   PASS  one tile of one large segment for digit pass p: the onesweep tile
-//         of the plain sort (pa_onesweep_tile.cuh), look-back within the
-//         segment;
+//   PASS  (11-bit plans) one tile of one large segment for digit pass p: the
+//         onesweep tile of the plain sort (pa_onesweep_tile.cuh), look-back
+//         within the segment.  8-bit plans run each pass as its own launch
+//         after the persistent kernel instead (seg_pass_kernel: the plain
+//         sort's pass geometry over all large segments' tiles at once, no
+//         work-queue round trips per tile);
 //   SMALL one small segment (<= the small/large cutoff) sorted entirely in
 //         shared memory by eight stable 4-bit counting passes, read once and
 //         written once.
@@ -214,6 +217,51 @@ __global__ void __launch_bounds__(kBlock, 2) segsort_kernel(const PlanDev P) {
   }
 }
 
+// One digit pass over every large segment of an 8-bit plan: tiles taken in
+// launch order (ticket), each mapped to its segment through the plan's tile
+// table; the onesweep tile of the plain sort with the segment as the array,
+// so the look-back stays inside the segment (its first tile publishes an
+// INCLUSIVE word).  Runs after the persistent kernel has finished every
+// HIST and SCAN item, so no item waits.
+using PassGeometry = Geometry<uint32_t, false, kPassBlock, kPassItems>;
+
+__global__ void __launch_bounds__(kPassBlock, 3) seg_pass_kernel(const PlanDev P, uint32_t pass) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + PassGeometry::kBarOff);
+  uint32_t* s_tile = reinterpret_cast<uint32_t*>(smem + PassGeometry::kTileIdOff);
+  if (threadIdx.x == 0) {
+    *s_tile = atomicAdd(P.pass_ticket, 1u);
+    mbar_init(s_bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const uint32_t g = *s_tile;
+  if (g >= P.pass_tiles) {  // a ticket counter that was not cleared
+    if (threadIdx.x == 0) raise_error(P.err, DEVERR_BAD_STATE);
+    return;
+  }
+  const uint32_t seg = P.tile_seg[g];
+  const LargeSeg L = P.large[seg];
+  const bool even = (pass & 1u) == 0;
+  TileJob<uint32_t, uint32_t> job;
+  job.in = (even ? P.keys : P.tmp) + L.base;
+  job.out = (even ? P.tmp : P.keys) + L.base;
+  job.vin = nullptr;
+  job.vout = nullptr;
+  job.n = L.len;
+  job.out_n = L.len;
+  job.tile = g - L.ptile_base;
+  job.shift = 8u * pass;
+  job.tin = false;
+  job.tout = false;
+  job.bin_start = P.bin_start + (size_t)seg * 4 * 256 + pass * 256;
+  job.status = P.pass_status + (size_t)L.ptile_base * 256;
+  job.err = P.err;
+  job.spin_limit = kSpinLimit;
+  uint32_t parity = 0;
+  onesweep_tile_multisplit<uint32_t, false, kPassBlock, kPassItems, uint32_t>(job, smem, s_bar, parity);
+}
+
 // ---- host side ---------------------------------------------------------------
 template <int PI, int SI, int RB>
 constexpr size_t smem_bytes_for() {
@@ -276,6 +324,9 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
   hp->kc = kc;
   hp->passes = (uint32_t)passes;
   hp->radix_bits = (uint32_t)c.digit_bits;
+  hp->split = c.digit_bits == 8;
+  hp->tile_seg.clear();
+  hp->pass_tiles = 0;
   hp->off.assign(off, off + num_segments + 1);
   hp->items.clear();
   hp->large.clear();
@@ -294,6 +345,12 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
       L.hist_chunks = (uint32_t)((len + kHistChunk - 1) / kHistChunk);
       L.tile_base = total_tiles;
       total_tiles += L.tiles;
+      if (hp->split) {
+        const uint32_t pt = (uint32_t)((len + kPassTile - 1) / kPassTile);
+        L.ptile_base = hp->pass_tiles;
+        hp->pass_tiles += pt;
+        hp->tile_seg.insert(hp->tile_seg.end(), pt, (uint32_t)hp->large.size());
+      }
       hp->large.push_back(L);
     }
   }
@@ -302,7 +359,8 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
                    [&](uint32_t a, uint32_t b) { return off[a + 1] - off[a] > off[b + 1] - off[b]; });
   auto& items = hp->items;
   size_t next_small = 0;
-  const size_t gaps = 1 + 1 + (size_t)passes;  // after HIST, SCAN, and each pass but the last
+  // small items go after HIST, after SCAN and (PASS items) after each pass but the last
+  const size_t gaps = hp->split ? 2 : 1 + 1 + (size_t)passes;
   auto add_small = [&](size_t share_of) {
     const size_t upto = std::min(small_ids.size(), (small_ids.size() * share_of + gaps - 1) / gaps);
     for (; next_small < upto; ++next_small) items.push_back({ITEM_SMALL, 0, small_ids[next_small], 0});
@@ -313,10 +371,12 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
   add_small(1);
   for (uint32_t l = 0; l < nlarge; ++l) items.push_back({ITEM_SCAN, 0, l, 0});
   add_small(2);
-  for (uint32_t p = 0; p < (uint32_t)passes; ++p) {
-    for (uint32_t l = 0; l < nlarge; ++l)
-      for (uint32_t t = 0; t < hp->large[l].tiles; ++t) items.push_back({ITEM_PASS, p, l, t});
-    add_small(3 + p);
+  if (!hp->split) {
+    for (uint32_t p = 0; p < (uint32_t)passes; ++p) {
+      for (uint32_t l = 0; l < nlarge; ++l)
+        for (uint32_t t = 0; t < hp->large[l].tiles; ++t) items.push_back({ITEM_PASS, p, l, t});
+      add_small(3 + p);
+    }
   }
   add_small(gaps);
   hp->total_tiles = total_tiles;
@@ -334,13 +394,16 @@ int build_host_plan(const uint64_t* off_host, size_t num_segments, const pa_segs
   hp->o_items = take(std::max<size_t>(items.size(), 1) * sizeof(Item));
   hp->o_off = take(hp->off.size() * 8);
   hp->o_large = take(nl * sizeof(LargeSeg));
+  hp->o_tile_seg = take(std::max<size_t>(hp->tile_seg.size(), 1) * 4);  // (the uploaded image ends here)
   const size_t per_seg = (size_t)seg_digits(hp->radix_bits) * seg_bins(hp->radix_bits);
   hp->o_bins = take(nl * per_seg * 8);
   hp->o_err = take(256);
-  hp->o_head = take(256);
+  hp->o_head = take(256);  // everything from here on is cleared per run
   hp->o_done = take(nl * kStages * 4);
   hp->o_hist = take(nl * per_seg * 4);
-  hp->o_status = take((size_t)passes * std::max<uint32_t>(total_tiles, 1) * seg_bins(hp->radix_bits) * 4);
+  hp->o_status = take(hp->split ? 0 : (size_t)passes * std::max<uint32_t>(total_tiles, 1) * seg_bins(hp->radix_bits) * 4);
+  hp->o_pticket = take(256);
+  hp->o_pstatus = take((size_t)std::max<uint32_t>(hp->pass_tiles, 1) * 256 * 4);
   hp->bytes = o;
   return PA_OK;
 }
@@ -362,12 +425,14 @@ PlanDev device_view(const HostPlan& hp, char* dev, uint32_t* keys, uint32_t* tmp
   d.bin_start = reinterpret_cast<unsigned long long*>(dev + hp.o_bins);
   d.err = reinterpret_cast<uint32_t*>(dev + hp.o_err);
   d.radix_bits = hp.radix_bits;
+  d.tile_seg = reinterpret_cast<const uint32_t*>(dev + hp.o_tile_seg);
+  d.pass_tiles = hp.pass_tiles;
+  d.pass_ticket = reinterpret_cast<uint32_t*>(dev + hp.o_pticket);
+  d.pass_status = reinterpret_cast<uint32_t*>(dev + hp.o_pstatus);
   return d;
 }
 
-size_t plan_image_bytes(const HostPlan& hp) {
-  return hp.o_large + std::max<size_t>(hp.large.size(), 1) * sizeof(LargeSeg);
-}
+size_t plan_image_bytes(const HostPlan& hp) { return hp.o_tile_seg + std::max<size_t>(hp.tile_seg.size(), 1) * 4; }
 
 cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s, void* pinned_staging) {
   cudaError_t e = cudaSuccess;
@@ -378,6 +443,7 @@ cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s, void* pin
     if (!hp.items.empty()) std::memcpy(img + hp.o_items, hp.items.data(), hp.items.size() * sizeof(Item));
     std::memcpy(img + hp.o_off, hp.off.data(), hp.off.size() * 8);
     if (!hp.large.empty()) std::memcpy(img + hp.o_large, hp.large.data(), hp.large.size() * sizeof(LargeSeg));
+    if (!hp.tile_seg.empty()) std::memcpy(img + hp.o_tile_seg, hp.tile_seg.data(), hp.tile_seg.size() * 4);
     e = cudaMemcpyAsync(dev, img, bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(dev + hp.o_err, 0, 256, s);
     return e;
@@ -389,12 +455,15 @@ cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s, void* pin
   if (e == cudaSuccess && !hp.large.empty())
     e = cudaMemcpyAsync(dev + hp.o_large, hp.large.data(), hp.large.size() * sizeof(LargeSeg),
                         cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && !hp.tile_seg.empty())
+    e = cudaMemcpyAsync(dev + hp.o_tile_seg, hp.tile_seg.data(), hp.tile_seg.size() * 4, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(dev + hp.o_err, 0, 256, s);
   return e;
 }
 
 unsigned plan_grid(const HostPlan& hp) {
   if (ensure_dynamic_smem(hp.kc.fn, hp.kc.smem) != cudaSuccess) cudaGetLastError();  // the launch reports it
+  if (hp.split && ensure_dynamic_smem(seg_pass_kernel, PassGeometry::kBytes) != cudaSuccess) cudaGetLastError();
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hp.kc.fn, kBlock, hp.kc.smem) != cudaSuccess) {
     cudaGetLastError();
@@ -407,10 +476,21 @@ unsigned plan_grid(const HostPlan& hp) {
 }
 
 cudaError_t launch_plan(const HostPlan& hp, const PlanDev& pd, char* dev, unsigned grid, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(dev + hp.o_head, 0, hp.bytes - hp.o_head, s);
-  if (e != cudaSuccess || hp.items.empty()) return e;
-  hp.kc.fn<<<grid, kBlock, hp.kc.smem, s>>>(pd);
-  return cudaGetLastError();
+  cudaError_t e = cudaMemsetAsync(dev + hp.o_head, 0, hp.o_pticket - hp.o_head, s);
+  if (e != cudaSuccess) return e;
+  if (!hp.items.empty()) {
+    hp.kc.fn<<<grid, kBlock, hp.kc.smem, s>>>(pd);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  if (!hp.split || hp.pass_tiles == 0) return cudaSuccess;
+  for (uint32_t p = 0; p < hp.passes && e == cudaSuccess; ++p) {
+    e = cudaMemsetAsync(dev + hp.o_pticket, 0, hp.bytes - hp.o_pticket, s);
+    if (e == cudaSuccess) {
+      seg_pass_kernel<<<hp.pass_tiles, kPassBlock, PassGeometry::kBytes, s>>>(pd, p);
+      e = cudaGetLastError();
+    }
+  }
+  return e;
 }
 
 }  // namespace seg

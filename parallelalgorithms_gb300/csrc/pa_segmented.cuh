@@ -35,8 +35,18 @@ struct LargeSeg {
   uint32_t len;
   uint32_t tiles;
   uint32_t hist_chunks;
-  uint32_t tile_base;  // first tile of this segment in each pass's status array
+  uint32_t tile_base;   // first tile of this segment in each pass's status array (PASS items)
+  uint32_t ptile_base;  // first tile of this segment in a pass launch (8-bit plans)
+  uint32_t pad;
 };
+
+// 8-bit plans run their digit passes as separate launches after the
+// persistent kernel: one onesweep launch per pass over every large
+// segment's tiles (the plain sort's pass geometry), look-back within each
+// segment.
+constexpr int kPassBlock = 384;
+constexpr int kPassItems = 16;
+constexpr uint32_t kPassTile = (uint32_t)kPassBlock * kPassItems;
 
 struct PlanDev {
   uint32_t* keys;
@@ -55,6 +65,11 @@ struct PlanDev {
   unsigned long long* bin_start;   // [large][digits][bins]
   uint32_t* err;
   uint32_t radix_bits;             // 8 (256 bins, 4 digits) or 11 (2048 bins, 3 digits)
+  // pass launches (8-bit plans)
+  const uint32_t* tile_seg;        // [pass_tiles] large segment of each tile
+  uint32_t pass_tiles;
+  uint32_t* pass_ticket;           // zeroed before each pass
+  uint32_t* pass_status;           // [pass_tiles][256], zeroed before each pass
 };
 
 // Digits of a 32-bit key and bins per digit for a digit width.
@@ -83,8 +98,11 @@ struct HostPlan {
   uint32_t passes = kPasses;  // digit passes of the large segments (3: every segment's top byte is
                               // constant; 3 with 11-bit digits)
   uint32_t radix_bits = 8;
-  size_t o_items = 0, o_off = 0, o_large = 0, o_bins = 0, o_err = 0, o_head = 0, o_done = 0, o_hist = 0,
-         o_status = 0, bytes = 0;
+  bool split = false;              // digit passes as separate launches (8-bit plans)
+  uint32_t pass_tiles = 0;
+  std::vector<uint32_t> tile_seg;
+  size_t o_items = 0, o_off = 0, o_large = 0, o_tile_seg = 0, o_bins = 0, o_err = 0, o_head = 0, o_done = 0,
+         o_hist = 0, o_status = 0, o_pticket = 0, o_pstatus = 0, bytes = 0;
 };
 
 // Validates the offsets and plans the queue and the device block layout.
@@ -109,7 +127,8 @@ cudaError_t upload_plan(const HostPlan& hp, char* dev, cudaStream_t s, void* pin
 size_t plan_image_bytes(const HostPlan& hp);
 // Persistent grid for the plan's kernel on the current device.
 unsigned plan_grid(const HostPlan& hp);
-// Clears the per-run state and launches the persistent kernel.
+// Clears the per-run state and launches the persistent kernel (and, for an
+// 8-bit plan, the pass launches after it).
 cudaError_t launch_plan(const HostPlan& hp, const PlanDev& pd, char* dev, unsigned grid, cudaStream_t s);
 
 }  // namespace seg
