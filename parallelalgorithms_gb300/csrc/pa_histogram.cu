@@ -43,9 +43,12 @@ constexpr size_t hist_smem_bytes() {
   return (size_t)ND * (1 << RB) * kLanes<ND, RB> * 4;
 }
 
-template <typename K, int ND, int RB>
+// BYTES: the digits are the key's bytes shift0 / 8, shift0 / 8 + 1, ... (the
+// sorts' histograms): each is extracted by one byte permute instead of a
+// shift and a mask.  FLT: 32-bit float keys, counted in their ordered form.
+template <typename K, int ND, int RB, bool BYTES, bool FLT>
 __global__ void __launch_bounds__(kHistBlock, 1) digit_counts_kernel(const K* __restrict__ keys, size_t n,
-                                                                       uint32_t shift0, uint32_t step, int is_float,
+                                                                       uint32_t shift0, uint32_t step,
                                                                        unsigned long long* __restrict__ out) {
   constexpr int R = 1 << RB;
   constexpr int V = kVec<K>;
@@ -56,13 +59,24 @@ __global__ void __launch_bounds__(kHistBlock, 1) digit_counts_kernel(const K* __
   __syncthreads();
   const uint32_t lane = threadIdx.x % L;
   uint32_t* my = s_h + lane;
-  const bool flt = is_float != 0;
+  const uint32_t byte0 = shift0 / 8;
 
   auto count = [&](K key) {
-    if (sizeof(K) == 4) key = to_ordered(key, flt);
+    if constexpr (sizeof(K) == 4 && FLT) key = to_ordered(key, true);
 #pragma unroll
     for (int d = 0; d < ND; ++d) {
-      const uint32_t b = (uint32_t)(key >> (shift0 + (uint32_t)d * step)) & (R - 1);
+      uint32_t b;
+      if constexpr (BYTES && RB == 8) {
+        const uint32_t byte = byte0 + (uint32_t)d;
+        if constexpr (sizeof(K) == 8)
+          b = __byte_perm(byte < 4 ? (uint32_t)key : (uint32_t)(key >> 32), 0u, 0x4440u | (byte & 3u));
+        else if constexpr (sizeof(K) == 4)
+          b = __byte_perm((uint32_t)key, 0u, 0x4440u | (byte & 3u));
+        else
+          b = (uint32_t)key;
+      } else {
+        b = (uint32_t)(key >> (shift0 + (uint32_t)d * step)) & (R - 1);
+      }
       atomicAdd(my + ((uint32_t)d * R + b) * L, 1u);
     }
   };
@@ -107,20 +121,30 @@ __global__ void __launch_bounds__(kHistBlock, 1) digit_counts_kernel(const K* __
   }
 }
 
-template <typename K, int ND, int RB>
-cudaError_t launch_counts_t(const void* keys, size_t n, uint32_t shift0, uint32_t step, bool is_float,
-                            unsigned long long* out, cudaStream_t stream) {
+template <typename K, int ND, int RB, bool BYTES, bool FLT>
+cudaError_t launch_counts_k(const void* keys, size_t n, uint32_t shift0, uint32_t step, unsigned long long* out,
+                            cudaStream_t stream) {
   constexpr int V = kVec<K>;
-  auto kern = digit_counts_kernel<K, ND, RB>;
+  auto kern = digit_counts_kernel<K, ND, RB, BYTES, FLT>;
   constexpr size_t smem = hist_smem_bytes<ND, RB>();
   cudaError_t e = ensure_dynamic_smem(kern, smem);
   if (e != cudaSuccess) return e;
   const size_t work = ceil_div(ceil_div(n, (size_t)V), (size_t)kHistBlock * 4);
   size_t blocks = work < (size_t)device_info().sm_count ? work : (size_t)device_info().sm_count;
   if (blocks < 1) blocks = 1;
-  kern<<<(unsigned)blocks, kHistBlock, smem, stream>>>(static_cast<const K*>(keys), n, shift0, step,
-                                                       is_float ? 1 : 0, out);
+  kern<<<(unsigned)blocks, kHistBlock, smem, stream>>>(static_cast<const K*>(keys), n, shift0, step, out);
   return cudaGetLastError();
+}
+
+template <typename K, int ND, int RB>
+cudaError_t launch_counts_t(const void* keys, size_t n, uint32_t shift0, uint32_t step, bool is_float,
+                            unsigned long long* out, cudaStream_t stream) {
+  const bool bytes = RB == 8 && shift0 % 8 == 0 && (ND == 1 || step == 8) && (sizeof(K) > 1 || shift0 == 0);
+  if (sizeof(K) == 4 && is_float)
+    return bytes ? launch_counts_k<K, ND, RB, true, true>(keys, n, shift0, step, out, stream)
+                 : launch_counts_k<K, ND, RB, false, true>(keys, n, shift0, step, out, stream);
+  return bytes ? launch_counts_k<K, ND, RB, true, false>(keys, n, shift0, step, out, stream)
+               : launch_counts_k<K, ND, RB, false, false>(keys, n, shift0, step, out, stream);
 }
 
 // Several arrays' one-digit histograms in one launch: CTAs walk the
