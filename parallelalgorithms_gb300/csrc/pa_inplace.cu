@@ -38,10 +38,9 @@ namespace {
 
 constexpr int kBins = 256;
 constexpr int kPlanThreads = kBins;  // plan kernels: one thread per bucket
-constexpr int kMoveBlock = 256;
-constexpr int kMoveItems = 16;
-constexpr int kMoveTile = kMoveBlock * kMoveItems;
+constexpr int kMoveBlock = 256;  // threads of the copy kernel (and of the plan kernels' scans)
 constexpr int kMoveWarps = kMoveBlock / 32;
+static_assert(kMoveBlock == kPlanThreads, "the block scan serves both");
 
 // Exclusive prefix of v over the 256 threads of the CTA; *total = the sum.
 // s_warp: 8 words of shared memory.  Contains barriers: every thread calls it.
