@@ -71,7 +71,7 @@ def parse_args():
     # seeded input and prints no JSON line (the commands in profiles/ use it)
     p.add_argument("--profile-op", default=None,
                    choices=["sort_u32", "sort_u32_host", "sort_u64", "sort_kv_u64", "sort_f32", "hist_u32",
-                            "select_u32", "sum_u32", "sort_u32_inplace", "partition_u32"])
+                            "select_u32", "sum_u32", "sort_u32_inplace", "partition_u32", "batched_c4"])
     p.add_argument("--reps", type=int, default=2)
     # the serving stream alone (the default run measures it in a child
     # process of its own, started this way)
@@ -88,7 +88,8 @@ def profile_op(a) -> None:
     one scan, one onesweep launch per key byte, one final copy.
     `sort_u32_host` sorts a page-locked host copy through the C ABI instead
     (the pipelined host-buffer path); `sort_u32_inplace` is the bounded-scratch
-    in-place sort, `partition_u32` PartitionRadix around k = n/2 and n - 21."""
+    in-place sort, `partition_u32` PartitionRadix around k = n/2 and n - 21,
+    `batched_c4` one run of the batched segmented sort on the C4 arrays."""
     import torch
 
     from parallelalgorithms_gb300 import _native, build, workloads
@@ -119,6 +120,19 @@ def profile_op(a) -> None:
         host_t = torch.empty(n, dtype=torch.int32, pin_memory=True)  # (kept alive for the view below)
         host = host_t.numpy().view(np.uint32)
     op = a.profile_op
+    if op == "batched_c4":  # the C4 segmentation (4096 arrays, 2.0 G keys), default plan; --n is not used
+        from parallelalgorithms_gb300 import batched
+        del src, k, t
+        sizes = workloads.log_uniform_sizes(4096, 1e3, 4e6)
+        off = np.zeros(sizes.size + 1, np.uint64)
+        off[1:] = np.cumsum(sizes)
+        c4_src = torch.from_numpy(workloads.uniform_u32(int(off[-1]), seed=workloads.SEED_SEGMENT_SIZES)
+                                  .view(np.int32)).cuda()
+        c4_keys = c4_src.clone()
+        c4_tmp = torch.empty_like(c4_src)
+        c4_plan = batched.SegmentedSortPlan(off, use_graph=False)
+        k = c4_keys
+        src = c4_src
     for _ in range(a.reps):
         k.copy_(src)
         if op == "sort_u32_host":
@@ -140,6 +154,8 @@ def profile_op(a) -> None:
             _native.call("pa_sum_u32", P(k.data_ptr()), n, P(out.data_ptr()), o)
         elif op == "sort_u32_inplace":
             _native.call("pa_sort_u32_inplace", P(k.data_ptr()), n, 0, o)
+        elif op == "batched_c4":
+            c4_plan.run(c4_keys, c4_tmp, torch.cuda.current_stream().cuda_stream)
         elif op == "partition_u32":
             ks = np.array([n // 2, n - 21], np.uint64)
             _native.call("pa_partition_radix_u32", P(k.data_ptr()), n, P(ks.ctypes.data), ks.size, o)
