@@ -84,3 +84,24 @@ def test_budget_admission_and_rejection(pa, torch_cuda):
     for r in small:
         k = r.keys
         assert np.all(k[1:] >= k[:-1])
+
+
+def test_join_limits(pa, port, torch_cuda):
+    """Requests above the join limit run alone; invalid limits are refused."""
+    from parallelalgorithms_gb300 import serving
+    with pytest.raises(pa.PaError):
+        serving.Server(join_max_keys_log2=41)
+    with pytest.raises(pa.PaError):
+        serving.Server(unit_max_keys_log2=-1)
+    specs = serving.make_specs(40, seed=13, lo=1e2, hi=1e5)
+    bufs = serving.materialize(specs)
+    with serving.Server(max_inflight=2, join_max_keys_log2=10, unit_max_keys_log2=12) as srv:
+        reqs = serving.run_served(srv, specs, bufs, rate=None)
+        st = srv.stats()
+    assert st["completed"] == len(specs)
+    for s, r, (buf, _, src) in zip(specs, reqs, bufs):
+        assert r.c.status == 0
+        if s.n > 1024:
+            assert r.c.unit_size == 1
+        if s.op == serving.REQ_SORT:
+            np.testing.assert_array_equal(buf, port.sort(src)[0])
