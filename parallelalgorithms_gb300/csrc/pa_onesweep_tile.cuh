@@ -830,7 +830,6 @@ __device__ __forceinline__ void onesweep_tile_wide(const TileJob<K, S>& job, uns
   constexpr int WARPS = G::kWarps;
   constexpr int R = G::kBins;
   constexpr int BPT = R / BLOCK;  // bins per thread
-  constexpr uint32_t FULL = 0xFFFFFFFFu;
   K* s_keys = reinterpret_cast<K*>(smem + G::kKeysOff);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + G::kValsOff);
   uint16_t* s_wh = reinterpret_cast<uint16_t*>(smem + G::kWhOff);
