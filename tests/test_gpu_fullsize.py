@@ -116,3 +116,36 @@ def test_batched_4096_arrays_200m(pa, port, torch_cuda):
         want, _ = port.sort(keys[a:b])
         np.testing.assert_array_equal(got[a:b], want, err_msg=f"segment {i}")
     plan.close()
+
+
+def test_u32_above_2_30_keys_plain_and_inplace(pa, torch_cuda):
+    """2^30 + 3 keys: the sorts' 64-bit look-back words (the plain sort's and
+    the in-place sort's scatter passes) and 64-bit positions, checked through
+    size-independent properties on the device: sorted, and every byte
+    histogram unchanged by the permutation."""
+    import ctypes
+    torch = torch_cuda
+    n = (1 << 30) + 3
+    P = ctypes.c_void_p
+    g = torch.Generator(device="cuda").manual_seed(1301)
+    src = torch.randint(-2 ** 31, 2 ** 31, (n,), dtype=torch.int32, device="cuda", generator=g)
+    hist = torch.zeros(1024, dtype=torch.int64, device="cuda")
+    pa.call("pa_hist_byte_components_u32", P(src.data_ptr()), n, P(hist.data_ptr()), None)
+    want_hist = hist.clone()
+    flip = torch.tensor(-2 ** 31, dtype=torch.int32, device="cuda")  # order-preserving signed view
+
+    def check(d):
+        f = d ^ flip
+        assert bool(torch.all(f[1:] >= f[:-1]))
+        hist.zero_()
+        pa.call("pa_hist_byte_components_u32", P(d.data_ptr()), n, P(hist.data_ptr()), None)
+        assert torch.equal(hist, want_hist)
+
+    d = src.clone()
+    tmp = torch.empty_like(d)
+    pa.call("pa_sort_u32", P(d.data_ptr()), P(tmp.data_ptr()), n, None)
+    check(d)
+    del tmp
+    d.copy_(src)
+    pa.call("pa_sort_u32_inplace", P(d.data_ptr()), n, 0, None)
+    check(d)
