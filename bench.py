@@ -680,7 +680,32 @@ def serving_extra(count: int = 120) -> dict:
     h2d = sum(s.n * (4 if s.key_kind == serving.KEY_U32 else 8) for s in specs)
     d2h = sum(s.n * (4 if s.key_kind == serving.KEY_U32 else 8) for s in specs if s.op == serving.REQ_SORT)
     out["host_link_bytes"] = {"h2d": h2d, "d2h": d2h}
+    out["host_link_gbs"] = host_link_gbs()
     return out
+
+
+def host_link_gbs() -> dict:
+    """Copy-engine bandwidth of this GPU's host link, GB/s: eight 256 MB
+    page-locked copies on eight streams, host to device, device to host, and
+    half each way at once (the overlap the server's streams rely on)."""
+    import torch
+    nbytes = 256 << 20
+    hs = [torch.empty(nbytes, dtype=torch.uint8, pin_memory=True) for _ in range(8)]
+    ds = [torch.empty(nbytes, dtype=torch.uint8, device="cuda") for _ in range(8)]
+    streams = [torch.cuda.Stream() for _ in range(8)]
+    res = {}
+    for mode in ("h2d", "d2h", "both_ways"):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for i in range(8):
+            with torch.cuda.stream(streams[i]):
+                if mode == "h2d" or (mode == "both_ways" and i % 2 == 0):
+                    ds[i].copy_(hs[i], non_blocking=True)
+                else:
+                    hs[i].copy_(ds[i], non_blocking=True)
+        torch.cuda.synchronize()
+        res[mode] = round(8 * nbytes / (time.perf_counter() - t) / 1e9, 1)
+    return res
 
 
 def run_extras(pa, lib, _native, workloads, n, stream, peak) -> dict:
