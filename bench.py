@@ -681,6 +681,7 @@ def serving_extra(count: int = 120) -> dict:
     d2h = sum(s.n * (4 if s.key_kind == serving.KEY_U32 else 8) for s in specs if s.op == serving.REQ_SORT)
     out["host_link_bytes"] = {"h2d": h2d, "d2h": d2h}
     out["host_link_gbs"] = host_link_gbs()
+    out["host_buffers_page_locked"] = all(keep is not None and keep.is_pinned() for _, keep, _ in bufs)
     return out
 
 
