@@ -628,11 +628,14 @@ def serving_extra(count: int = 120) -> dict:
     # all requests waiting at once (the throughput comparison): one measured
     # run on each of five servers created one after another, median reported
     sat = []
-    for _ in range(5):
-        with serving.Server(**kw) as srv:
-            serving.run_served(srv, specs, bufs, None)  # warm the server's pinned staging blocks
-            reqs = serving.run_served(srv, specs, bufs, None)
-            sat.append((span_of(reqs), reqs, srv.stats()))
+    import torch
+    sampler = ClockSampler(torch.cuda.current_device())
+    with sampler:  # SM clocks and throttle reasons while the servers run
+        for _ in range(5):
+            with serving.Server(**kw) as srv:
+                serving.run_served(srv, specs, bufs, None)  # warm the server's pinned staging blocks
+                reqs = serving.run_served(srv, specs, bufs, None)
+                sat.append((span_of(reqs), reqs, srv.stats()))
     in_order = [x[0] for x in sat]
     sat.sort(key=lambda x: x[0])
     span, reqs, sat_stats = sat[len(sat) // 2]
@@ -643,7 +646,7 @@ def serving_extra(count: int = 120) -> dict:
                                 "speedup_all_servers": sorted(plain_s / x for x in spans),
                                 "makespans_s": spans, "makespans_s_in_creation_order": in_order,
                                 "servers": len(sat),
-                                "server_stats": sat_stats,
+                                "server_stats": sat_stats, "clocks": sampler.summary(),
                                 "shared_unit_requests_share": sat_stats["coalesced_requests"] / max(1, sat_stats["completed"])}
     with serving.Server(**kw) as srv:
         serving.run_served(srv, specs, bufs, None)  # warm the server's pinned staging blocks
