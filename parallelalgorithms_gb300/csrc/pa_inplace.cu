@@ -177,17 +177,27 @@ __global__ void __launch_bounds__(kMoveBlock) inplace_gather_kernel(const uint32
     const uint32_t cn = (uint32_t)min((unsigned long long)kGatherChunk, end - c0);
     const uint32_t b_lo = run_of(c0, 0);
     const uint32_t b_hi = run_of(c0 + cn - 1, b_lo);
+    // every load of the chunk first (all in flight together), then the stores
+    uint32_t kk[kGatherItems];
 #pragma unroll
     for (int j = 0; j < kGatherItems; ++j) {
       const uint32_t o = (uint32_t)j * kMoveBlock + tid;
-      const bool valid = o < cn;
-      uint32_t k = 0;
-      if (valid) {
+      kk[j] = 0;
+      if (o < cn) {
         const unsigned long long i = c0 + o;
         const uint32_t b = b_lo == b_hi ? b_lo : run_of(i, b_lo);
-        k = keys[s_src[b] + (i - s_dst[b])];
-        dst[i] = k;
+        kk[j] = keys[s_src[b] + (i - s_dst[b])];
       }
+    }
+#pragma unroll
+    for (int j = 0; j < kGatherItems; ++j) {
+      const uint32_t o = (uint32_t)j * kMoveBlock + tid;
+      if (o < cn) dst[c0 + o] = kk[j];
+    }
+#pragma unroll
+    for (int j = 0; j < kGatherItems; ++j) {
+      const bool valid = (uint32_t)j * kMoveBlock + tid < cn;
+      const uint32_t k = kk[j];
       // digit counts; a warp whose keys share one digit (skewed inputs) adds
       // them with one atomic instead of 32 on the same word
       // (every lane runs the shuffle: a full-mask collective skipped by some
