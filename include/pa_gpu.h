@@ -134,7 +134,9 @@ int pa_sort_u32_noalloc(uint32_t* keys, uint32_t* tmp, size_t n, const pa_opts* 
  * buckets of at most scratch_keys keys are sorted in groups by the batched
  * segmented sort.  Same sorted array as pa_sort_u32.  For keys above 2^24
  * the call waits for the device once per partitioned range (it reads the
- * range's digit counts back to plan the buckets). */
+ * range's digit counts back to plan the buckets).  If it fails part way,
+ * device keys may be left partly moved (keys in flight through the scratch
+ * are not put back); host keys are left as they were. */
 int pa_sort_u32_inplace(uint32_t* keys, size_t n, size_t scratch_keys, const pa_opts* opts);
 
 /* ---- digit histograms ----------------------------------------------------
