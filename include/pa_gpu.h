@@ -219,16 +219,19 @@ int pa_sum_chunked(const void* a, size_t n, int elem_kind, size_t chunk, uint64_
  * No reference counterpart (the reference sorts one array per call).  Sorts
  * every segment [seg_offsets[i], seg_offsets[i + 1]) of one uint32 key array
  * independently (stable, ascending; each segment's result equals
- * pa_sort_u32 on it) in ONE persistent kernel launch fed by a device work
- * queue: segments up to `small_cutoff` keys are sorted inside one CTA's
- * shared memory, longer ones by the onesweep passes.  A plan is built once
+ * pa_sort_u32 on it): a persistent kernel fed by a device work queue sorts
+ * the segments of up to `small_cutoff` keys inside one CTA's shared memory
+ * and counts the longer ones' digits, then (8-bit digits) one onesweep launch
+ * per digit pass covers every longer segment (11-bit digits: the passes run
+ * as items of the persistent kernel).  A plan is built once
  * for a segmentation and replayed (through a captured CUDA graph when
  * use_graph is set); pa_segmented_sort_u32 is the one-shot form.  Segments
  * must be shorter than 2^30 keys.
  */
 typedef struct pa_segsort_config {
   int small_cutoff;  /* 0 (= 4096), 2048, 4096 or 8192 keys */
-  int tile_keys;     /* onesweep tile for longer segments: 0 (= 8192), 4096 or 8192 */
+  int tile_keys;     /* onesweep tile of 11-bit plans: 0 (= 8192), 4096 or 8192 (8-bit
+                        plans' pass launches use the plain sort's 6144-key tile) */
   int digit_bits;    /* 0 or 8 (four passes), or 11 (three passes of 2048 bins;
                         the result is copied back from tmp) */
   int use_graph;     /* 1: plan runs replay a captured CUDA graph */

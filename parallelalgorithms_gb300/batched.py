@@ -7,10 +7,11 @@ sorted inside one CTA's shared memory, longer ones by the onesweep passes.
 A plan is built once per segmentation and replayed through a captured CUDA
 graph.
 
-The autotuner times every candidate configuration (small/large cutoff,
-onesweep tile size; 8-bit digits) on the caller's own data and remembers the
-fastest per (GPU, workload shape) in a JSON file, so later plans for the same
-shape start from the tuned choice without measuring again.
+The autotuner times every candidate configuration (small/large cutoff and
+digit width; the onesweep tile of 11-bit plans) on the caller's own data and
+remembers the fastest per (GPU, workload shape) in a JSON file, so later
+plans for the same shape start from the tuned choice without measuring
+again.
 """
 from __future__ import annotations
 
@@ -45,9 +46,10 @@ class SegSortChoice:
         return c
 
 
-# small/large cutoff x tile with 8-bit digits, and 11-bit digits (three
-# passes of 2048 bins) at the default cutoff
-CANDIDATES = ([SegSortChoice(c, t) for c in (2048, 4096, 8192) for t in (4096, 8192)] +
+# the small/large cutoff with 8-bit digits (whose passes use the plain
+# sort's tile), and 11-bit digits (three passes of 2048 bins) at the default
+# cutoff with either tile
+CANDIDATES = ([SegSortChoice(c, 8192) for c in (2048, 4096, 8192)] +
               [SegSortChoice(4096, t, 11) for t in (4096, 8192)])
 
 
