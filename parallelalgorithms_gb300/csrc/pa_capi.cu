@@ -845,20 +845,28 @@ size_t sort_scratch_bytes(size_t n, int kb, bool has_vals, int radix_bits) {
 size_t sort_scratch_layout(char* base, size_t n, int kb, bool has_vals, SortScratch* s, int radix_bits) {
   const int passes = sort_passes(kb, radix_bits);
   const size_t bins = (size_t)1 << radix_bits;
-  const size_t tiles = ceil_div(n, onesweep_tile_keys(kb, has_vals, radix_bits));
+  const size_t tile_keys = onesweep_tile_keys(kb, has_vals, radix_bits);
+  const size_t tiles = ceil_div(n, tile_keys);
   const size_t sb = onesweep_status_bytes(n);
+  // the first pass's prepared offsets (launch_tile_counts)
+  const bool prepared = kb == 4 && !has_vals && radix_bits == 8 && n < ((size_t)1 << 30) && tiles >= 2 &&
+                        tile_counts_supported(tile_keys);
   Carve c{base};
   s->radix_bits = radix_bits;
   s->passes = passes;
   s->counts = c.take<unsigned long long>((size_t)passes * bins);
   s->zero_begin = reinterpret_cast<char*>(s->counts);
-  s->tile_ctr = c.take<uint32_t>(passes);
+  s->tile_ctr = c.take<uint32_t>((size_t)passes + 1);
+  s->tc_ticket = s->tile_ctr + passes;
   s->status = c.take<char>((size_t)passes * tiles * bins * sb);
   s->zero_bytes = (size_t)(base + c.off - s->zero_begin);
   s->bin_start = c.take<unsigned long long>((size_t)passes * bins);
   s->ctrl = c.take<SortCtrl>(1);
   s->tiles = tiles;
   s->status_bytes = sb;
+  s->tile_prefix = prepared ? c.take<uint32_t>(tiles * 256) : nullptr;
+  s->chunk_tot = prepared ? c.take<uint32_t>((size_t)kTileCountMaxChunks * 256) : nullptr;
+  s->chunk_excl = prepared ? c.take<uint32_t>((size_t)kTileCountMaxChunks * 256) : nullptr;
   return c.off;
 }
 
@@ -881,7 +889,16 @@ cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32
   }
   cudaError_t e = cudaMemsetAsync(s.zero_begin, 0, s.zero_bytes, stream);
   if (e == cudaSuccess) e = m();
-  if (e == cudaSuccess) e = launch_digit_counts(d_keys, n, kb, passes, rb, 0, (uint32_t)rb, is_float, s.counts, stream);
+  // With the tables (and 16-byte aligned keys) the histogram also prepares
+  // the first pass's tile offsets.
+  const bool prepared = s.tile_prefix && kb == 4 && rb == 8 && !has_vals && n < ((size_t)1 << 30) &&
+                        (reinterpret_cast<uintptr_t>(d_keys) & 15u) == 0;
+  uint32_t tpc = 0;
+  if (e == cudaSuccess)
+    e = prepared ? launch_tile_counts(static_cast<const uint32_t*>(d_keys), n, onesweep_tile_keys(kb, false, rb),
+                                      is_float, s.counts, s.tile_prefix, s.chunk_tot, s.chunk_excl, s.tc_ticket, &tpc,
+                                      stream)
+                 : launch_digit_counts(d_keys, n, kb, passes, rb, 0, (uint32_t)rb, is_float, s.counts, stream);
   if (e == cudaSuccess) e = m();
   if (e == cudaSuccess) e = launch_scan_digits(s.counts, passes, rb, n, is_float, true, s.bin_start, s.ctrl, stream);
   if (e == cudaSuccess) e = m();
@@ -901,6 +918,11 @@ cudaError_t enqueue_sort(const SortScratch& s, void* d_keys, void* d_tmp, uint32
     a.tile_counter = s.tile_ctr + p;
     a.ctrl = s.ctrl;
     a.err = err;
+    if (prepared && p == 0) {  // pass 0, when it runs, reads the keys the histogram read
+      a.tile_prefix = s.tile_prefix;
+      a.chunk_excl = s.chunk_excl;
+      a.tiles_per_chunk = tpc;
+    }
     e = launch_onesweep_pass(a, kb, has_vals, stream);
     if (e == cudaSuccess) e = m();
   }

@@ -62,6 +62,22 @@ cudaError_t launch_digit_counts(const void* keys, size_t n, int key_bytes, int n
                                 uint32_t shift0, uint32_t shift_step, bool is_float, unsigned long long* out,
                                 cudaStream_t stream);
 
+// The histogram of a 32-bit sort with 8-bit digits that also prepares its
+// first digit pass: one read of keys[0, n) (16-byte aligned, n < 2^30)
+// ADDS the counts of the four bytes into out[4][256] as launch_digit_counts
+// does, and, for the first pass's tiles of tile_keys keys (4096, 6144 or
+// 8192), writes
+//   tile_prefix[t][b]  keys of byte-0 value b in the earlier tiles of t's chunk,
+//   chunk_excl[c][b]   keys of byte-0 value b in the chunks before c,
+// where chunk c is the tiles [c * tpc, (c + 1) * tpc) (*tpc set here), so
+// that the pass finds each tile's offsets without a look-back.  chunk_tot
+// ([kTileCountMaxChunks][256]) is scratch; *ticket starts at zero.
+constexpr int kTileCountMaxChunks = 160;
+bool tile_counts_supported(size_t tile_keys);
+cudaError_t launch_tile_counts(const uint32_t* keys, size_t n, size_t tile_keys, bool is_float,
+                               unsigned long long* out, uint32_t* tile_prefix, uint32_t* chunk_tot,
+                               uint32_t* chunk_excl, uint32_t* ticket, uint32_t* tpc, cudaStream_t stream);
+
 // Several arrays' 256-bin histograms of (key >> shift) & 255 in one launch
 // (the serving loop's coalesced histogram requests).  jobs[0, njobs) in
 // device memory; job j's keys are split into kHistJobChunk-key chunks
@@ -123,6 +139,11 @@ struct OnesweepArgs {
   // output positions when the output is not an n-key array (0: n)
   const unsigned long long* n_dev = nullptr;
   size_t out_n = 0;
+  // First pass of a 32-bit keys-only sort: the tiles' offsets prepared by
+  // launch_tile_counts (each tile reads its two rows instead of looking back).
+  const uint32_t* tile_prefix = nullptr;
+  const uint32_t* chunk_excl = nullptr;
+  uint32_t tiles_per_chunk = 0;
 };
 
 // Tile geometry chosen for (key_bytes, has_vals, radix_bits); the workspace
@@ -189,6 +210,12 @@ struct SortScratch {
   size_t zero_bytes;
   size_t tiles;
   size_t status_bytes;
+  // launch_tile_counts' tables (32-bit keys only, 8-bit digits, n < 2^30;
+  // otherwise null): the first pass then needs no look-back
+  uint32_t* tile_prefix;
+  uint32_t* chunk_tot;
+  uint32_t* chunk_excl;
+  uint32_t* tc_ticket;  // zeroed with the counts
 };
 size_t sort_scratch_bytes(size_t n, int key_bytes, bool has_vals, int radix_bits = 8);
 // Carves the scratch from `base` (nullptr measures); returns its size.

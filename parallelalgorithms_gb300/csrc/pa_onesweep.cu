@@ -81,6 +81,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(const OnesweepArg
   job.status = static_cast<S*>(args.status);
   job.err = args.err;
   job.spin_limit = args.spin_limit ? args.spin_limit : kSpinLimit;
+  job.tile_prefix = args.tile_prefix;  // prepared offsets (used by the multisplit ranking)
+  job.chunk_excl = args.chunk_excl;
+  job.tiles_per_chunk = args.tiles_per_chunk;
   uint32_t parity = 0;
   if constexpr (MULTISPLIT)
     onesweep_tile_multisplit<K, HAS_VALS, BLOCK, ITEMS, S>(job, smem, s_bar, parity);

@@ -209,6 +209,13 @@ struct TileJob {
   S* status;
   uint32_t* err;
   uint32_t spin_limit;  // look-back polls before giving up (kSpinLimit unless a test lowers it)
+  // Prepared offsets (the first pass of a 32-bit keys-only sort, multisplit
+  // ranking only): bin b of this tile starts at bin_start[b] + tile_prefix[tile][b]
+  // + chunk_excl[tile / tiles_per_chunk][b]; the tile neither publishes nor
+  // looks back.
+  const uint32_t* tile_prefix = nullptr;
+  const uint32_t* chunk_excl = nullptr;
+  uint32_t tiles_per_chunk = 0;
 };
 
 // One tile of an onesweep digit pass (steps 2-6 above).  Called by all
@@ -459,6 +466,7 @@ struct TileSmem {
   uint32_t* tstart;  // [256] first in-tile position of each bin
   uint32_t* tcount;  // [256] keys of each bin in the tile
   uint32_t* abort;
+  uint32_t* pre = nullptr;  // [2][256]: the tile's prepared offset rows (tile_prefix, chunk_excl), if any
 };
 
 // Whether a pass can bulk-copy its tiles (16-byte aligned key and payload
@@ -471,20 +479,26 @@ __device__ __forceinline__ bool tile_tma_ok(const TileJob<K, S>& job) {
 
 // Starts the bulk copy of tile `tile` into `keys` / `vals`, completing on
 // `bar` (one thread calls it; the 16-byte multiple head of the tile only, the
-// body reads the ragged rest).  Nothing is issued for a pass that cannot
-// bulk-copy.
+// body reads the ragged rest), and with prepared offsets their two 1 KB rows
+// into `pre`.  Nothing is issued for a pass that cannot bulk-copy.
 template <typename K, bool HAS_VALS, int TILE, typename S>
 __device__ __forceinline__ void tile_issue_load(const TileJob<K, S>& job, uint32_t tile, K* keys, uint32_t* vals,
-                                                uint64_t* bar) {
+                                                uint64_t* bar, uint32_t* pre = nullptr) {
   if (!tile_tma_ok<K, HAS_VALS>(job)) return;
   const size_t tile_base = (size_t)tile * TILE;
   const uint32_t tile_n = (uint32_t)min((size_t)TILE, job.n - tile_base);
   const uint32_t kbulk = (tile_n * (uint32_t)sizeof(K)) & ~15u;
   const uint32_t vbulk = HAS_VALS ? ((tile_n * 4u) & ~15u) : 0u;
+  const bool prepared = pre != nullptr && job.tile_prefix != nullptr;
+  const uint32_t pbulk = prepared ? 2u * kRadix * 4u : 0u;
   fence_proxy_async();
-  mbar_arrive_expect_tx(bar, kbulk + vbulk);
+  mbar_arrive_expect_tx(bar, kbulk + vbulk + pbulk);
   if (kbulk) bulk_load_g2s(keys, job.in + tile_base, kbulk, bar);
   if (HAS_VALS && vbulk) bulk_load_g2s(vals, job.vin + tile_base, vbulk, bar);
+  if (prepared) {
+    bulk_load_g2s(pre, job.tile_prefix + (size_t)tile * kRadix, kRadix * 4u, bar);
+    bulk_load_g2s(pre + kRadix, job.chunk_excl + (size_t)(tile / job.tiles_per_chunk) * kRadix, kRadix * 4u, bar);
+  }
 }
 
 // Tuning switches of the multisplit ranking (compile-time):
@@ -557,6 +571,14 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
 
   // the ragged end (or, without bulk copies, everything) with plain loads
   const bool tma_ok = tile_tma_ok<K, HAS_VALS>(job);
+  // Prepared offsets: their rows came with the bulk copy, or are read here
+  // when the pass cannot bulk-copy (the barrier below orders either before use).
+  const bool prepared = job.tile_prefix != nullptr;  // (set only where sm.pre is)
+  if (prepared && !tma_ok)
+    for (uint32_t i = tid; i < (uint32_t)kRadix; i += BLOCK) {
+      sm.pre[i] = job.tile_prefix[(size_t)tile * kRadix + i];
+      sm.pre[kRadix + i] = job.chunk_excl[(size_t)(tile / job.tiles_per_chunk) * kRadix + i];
+    }
   uint32_t loaded = 0;
   if (tma_ok) {
     loaded = ((tile_n * (uint32_t)sizeof(K)) & ~15u) / (uint32_t)sizeof(K);
@@ -644,8 +666,10 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
       sum += c;
     }
     s_tcount[tid] = sum;
-    S* st = job.status + (size_t)tile * kRadix + tid;
-    st_relaxed_gpu(st, (S)((tile == 0 ? SW::kIncl : SW::kAgg) | (S)sum));
+    if (!prepared) {
+      S* st = job.status + (size_t)tile * kRadix + tid;
+      st_relaxed_gpu(st, (S)((tile == 0 ? SW::kIncl : SW::kAgg) | (S)sum));
+    }
   }
   __syncthreads();
   if (warp == 0) {  // exclusive scan of the 256 tile counts, 8 bins per lane
@@ -687,7 +711,9 @@ __device__ __forceinline__ void onesweep_tile_ms_body(const TileJob<K, S>& job, 
   if (tid < (uint32_t)kRadix) {
     const uint32_t count = s_tcount[tid];
     S excl = 0;
-    if (tile > 0) {
+    if (prepared) {
+      excl = (S)sm.pre[tid] + (S)sm.pre[kRadix + tid];
+    } else if (tile > 0) {
       const S* base = job.status + tid;
       long long t = (long long)tile - 1;
       uint32_t spins = 0;
@@ -1064,7 +1090,12 @@ __device__ __forceinline__ void onesweep_tile_multisplit(const TileJob<K, S>& jo
   sm.tstart = reinterpret_cast<uint32_t*>(smem + G::kBinStartOff);
   sm.tcount = reinterpret_cast<uint32_t*>(smem + G::kBinEndOff);
   sm.abort = reinterpret_cast<uint32_t*>(smem + G::kAbortOff);
-  if (threadIdx.x == 0) tile_issue_load<K, HAS_VALS, G::kTile>(job, job.tile, sm.keys, sm.vals, s_bar);
+  // the prepared offset rows sit in the counter area's last 2 KB, which the
+  // warp counters and match words leave free
+  static_assert((size_t)kMatchWords * G::kWarps * kRadix + 2 * kRadix <= (size_t)kNibbleBins * G::kCntRow,
+                "the prepared offset rows fit after the warp counters");
+  sm.pre = sm.wh + (size_t)kMatchWords * G::kWarps * kRadix;
+  if (threadIdx.x == 0) tile_issue_load<K, HAS_VALS, G::kTile>(job, job.tile, sm.keys, sm.vals, s_bar, sm.pre);
   onesweep_tile_ms_body<K, HAS_VALS, BLOCK, ITEMS, S>(job, sm, s_bar, parity);
 }
 
