@@ -127,8 +127,8 @@ int pa_sort_u32_noalloc(uint32_t* keys, uint32_t* tmp, size_t n, const pa_opts* 
  * parallel_hybrid_inplace_msd_radix_sort(a, a_size) (RadixSortMsdParallel.h:291),
  * whose point is to sort without a second array of n keys.  Besides the keys
  * (for host keys: their device copy) the call holds scratch_keys keys of
- * device scratch (0 = 2^24 = 64 MiB, at least 2^16) and about scratch_keys
- * / 2 + 8 MiB bytes of tables, whatever n is.  Up to scratch_keys keys it is
+ * device scratch (0 = 2^24 = 64 MiB, at least 2^16) and about 1.4 bytes per
+ * scratch key + 8 MiB of tables (31 MiB at the default), whatever n is.  Up to scratch_keys keys it is
  * the LSD sort with the scratch as its second buffer; above, ranges are
  * partitioned in place by a digit (top digit first) through the scratch and
  * buckets of at most scratch_keys keys are sorted in groups by the batched
