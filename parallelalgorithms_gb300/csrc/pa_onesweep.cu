@@ -24,7 +24,10 @@
 //      passes over the tile with per-thread counters (onesweep_tile);
 //   4. publish the tile's bin counts (AGGREGATE, or INCLUSIVE for tile 0);
 //   5. per bin, walk back over earlier tiles' words, four tiles per round
-//      trip, until an INCLUSIVE one; publish INCLUSIVE;
+//      trip, until an INCLUSIVE one; publish INCLUSIVE.  (The first pass of
+//      a 32-bit keys-only sort skips steps 4-5: its tiles' offsets were
+//      prepared by the histogram, launch_tile_counts, and arrive with the
+//      tile's bulk copy);
 //   6. stage the keys at their in-tile sorted position in shared memory and
 //      write them out: consecutive threads write consecutive keys of a bin to
 //      consecutive addresses.
